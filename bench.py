@@ -1,0 +1,398 @@
+"""Benchmark of the star-stencil sweep loop on one GB300 (or N replicas).
+
+Workload (one "step"): plain FP32 3-D star stencil, 512^3 grid, radius 1
+(7-point), Jacobi update (mean of the 6R axis neighbours), 1000 sweeps,
+border and interior i.i.d. uniform [0,1) from a seed.  The same loop at
+radius 4 (25-point) is reported as a second line item.  Metric: GCell-updates/s
+= (N - 2R)^3 * sweeps / seconds.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``--impl reference`` times the CPU restatement of the reference's sweep loop
+(the oracle, OpenMP over all host threads) on a bounded sample of the same
+workload: the reference's stencil_cpu itself is x86-built from its sources
+and does not exist on the GPU host.
+
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU
+(the path is a single-GPU solver: no collective); ``value`` sums the cell
+updates of all ranks over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIM = 512
+SWEEPS = 1000
+SEED = 20251203
+HBM_BYTES_PER_UPDATE = 8  # one FP32 read + one FP32 write per cell update
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--dim", type=int, default=DIM)
+    ap.add_argument("--sweeps", type=int, default=SWEEPS)
+    ap.add_argument("--radius", type=int, default=1)
+    ap.add_argument("--variant", default="auto")
+    ap.add_argument("--no-r4", action="store_true", help="skip the radius-4 line item")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            m = json.load(f)
+        return float(m["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(key):
+    """DRAM bytes per launch from the committed ncu summary (profiles/traffic.json)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(key)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join("/tmp", "stencil_clocks_%d_%d.csv" % (os.getpid(), gpu_index))
+
+    def __enter__(self):
+        try:
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.out.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx = float(parts[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        except OSError:
+            pass
+        try:
+            os.unlink(self.path)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def updates(dim, radius, sweeps):
+    return float(dim - 2 * radius) ** 3 * sweeps
+
+
+def time_device_loop(S, torch, u0, radius, sweeps, variant, steps, warmup, stream):
+    """Device-resident timing: inputs already in HBM.  Returns (seconds per step list,
+    launches per step)."""
+    from thesis_gb300 import lib
+    a = u0.clone()
+    b = u0.clone()
+    p = lib.make_params(tuple(u0.shape), radius, sweeps, lib.MODE_JACOBI, variant)
+    L = lib.load()
+    res = ctypes.c_void_p()
+
+    def step():
+        # each step restarts from the initial state (same work every step)
+        a.copy_(u0)
+        lib.check(L.stencil_dispatch_ex(ctypes.byref(p), ctypes.c_void_p(a.data_ptr()),
+                                        ctypes.c_void_p(b.data_ptr()),
+                                        ctypes.c_void_p(stream.cuda_stream), ctypes.byref(res)),
+                  "stencil_dispatch_ex")
+
+    with torch.cuda.stream(stream):
+        b.copy_(u0)
+        for _ in range(warmup):
+            step()
+        stream.synchronize()
+        times = []
+        for _ in range(steps):
+            # the restart copy is outside the event pair: only the sweeps are timed
+            a.copy_(u0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lib.check(L.stencil_dispatch_ex(ctypes.byref(p), ctypes.c_void_p(a.data_ptr()),
+                                            ctypes.c_void_p(b.data_ptr()),
+                                            ctypes.c_void_p(stream.cuda_stream),
+                                            ctypes.byref(res)), "stencil_dispatch_ex")
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+    del a, b
+    return times
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from thesis_gb300 import lib, stencil as S
+    from thesis_gb300 import build as B
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    if rank == 0 or world == 1:
+        B.build()
+    if world > 1:
+        dist.barrier()
+    lib.load()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(dev)
+    shape = (args.dim,) * 3
+    u0 = S.init_uniform(shape, SEED, device=dev)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def maxed(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- headline: device-resident sweeps (radius args.radius) ------------
+    barrier()
+    with ClockSampler(local) as clk:
+        barrier()
+        step_times = time_device_loop(S, torch, u0, args.radius, args.sweeps, args.variant,
+                                      args.steps, args.warmup, stream)
+        barrier()
+    total = maxed(sum(step_times))
+    ups = updates(args.dim, args.radius, args.sweeps)
+    value = ups * args.steps * world / total / 1e9
+    per_launch = min(step_times) / args.sweeps  # each sweep is one launch of the sweep kernel
+    peak, peak_kind = peaks()
+    achieved = ups / args.sweeps * HBM_BYTES_PER_UPDATE / per_launch / 1e9
+    traffic = profile_traffic("stream3d_r%d_512" % args.radius)
+
+    out = {
+        "metric": "GCell-updates/s (3D 512^3 FP32 star stencil, Jacobi, 1000 sweeps)",
+        "value": round(value, 3),
+        "unit": "GCell-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total / args.steps * 1e3, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic: border and interior i.i.d. uniform [0,1) (SplitMix64, seed %d)" % SEED,
+        "config": {"workload": "3D %d^3 FP32 star stencil R=%d, Jacobi, %d sweeps per step"
+                               % (args.dim, args.radius, args.sweeps),
+                   "dims": 3, "dim": args.dim, "radius": args.radius, "sweeps": args.sweeps,
+                   "variant": args.variant, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "no flush: 2 x %d MiB working set > 129 MB L2"
+                         % (args.dim ** 3 * 4 // 2 ** 20)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "bytes_per_update": HBM_BYTES_PER_UPDATE,
+                     "kernel_us_per_launch": round(per_launch * 1e6, 2)},
+        "gpu_launches": args.steps * args.sweeps,
+    }
+
+    # ---- radius-4 line item ---------------------------------------------
+    if not args.no_r4 and args.radius != 4:
+        barrier()
+        t4 = time_device_loop(S, torch, u0, 4, args.sweeps, args.variant,
+                              max(2, args.steps // 2), 2, stream)
+        t4s = maxed(sum(t4))
+        ups4 = updates(args.dim, 4, args.sweeps)
+        per4 = min(t4) / args.sweeps
+        ach4 = ups4 / args.sweeps * HBM_BYTES_PER_UPDATE / per4 / 1e9
+        out["r4"] = {"value": round(ups4 * len(t4) * world / t4s / 1e9, 3),
+                     "unit": "GCell-updates/s", "ms_per_step": round(t4s / len(t4) * 1e3, 3),
+                     "roofline": {"bound": "hbm", "achieved": round(ach4, 1), "peak": peak,
+                                  "unit": "GB/s", "frac": round(ach4 / peak, 4),
+                                  "traffic": profile_traffic("stream3d_r4_512")}}
+
+    # ---- end to end through the C ABI with host buffers --------------------
+    if not args.no_e2e:
+        h_in = u0.cpu().pin_memory()
+        h_out = torch.empty_like(h_in).pin_memory()
+        p = lib.make_params(shape, args.radius, args.sweeps, lib.MODE_JACOBI, args.variant)
+        L = lib.load()
+        ms = ctypes.c_float()
+
+        def e2e_step():
+            lib.check(L.stencil_run_host(ctypes.byref(p), ctypes.c_void_p(h_in.data_ptr()),
+                                         ctypes.c_void_p(h_out.data_ptr()), ctypes.byref(ms)),
+                      "stencil_run_host")
+
+        for _ in range(max(1, args.warmup - 1)):
+            e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        barrier()
+        te = maxed(time.perf_counter() - t0)
+        nbytes = h_in.numel() * 4
+        out["e2e"] = {"value": round(ups * args.steps * world / te / 1e9, 3),
+                      "unit": "GCell-updates/s", "h2d_bytes_per_step": nbytes,
+                      "d2h_bytes_per_step": nbytes,
+                      "api": "stencil_run_host (pinned host in/out, upload + sweeps + download)"}
+        L.stencil_release()
+
+    out["clocks"] = clk.summary()
+
+    # ---- CPU baseline: the oracle on the host cores, bounded sample -----------
+    if not args.no_cpu and rank == 0:
+        out["cpu_baseline"] = cpu_baseline(u0.cpu().numpy(), args.radius, target_s=10.0)
+
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def cpu_baseline(host_grid, radius, target_s=10.0, threads=None):
+    """Times the oracle's FP32 sweep (CPU restatement of src/stencil_cpu.cu) on
+    the host cores for about target_s seconds of sweeps over the full grid."""
+    import numpy as np
+    from oracle import oracle as O
+    threads = threads or os.cpu_count() or 1
+    a = np.ascontiguousarray(host_grid, np.float32).copy()
+    b = a.copy()
+    dim = a.shape[0]
+    t0 = time.perf_counter()
+    O.sweep(a, b, radius, O.JACOBI, threads)  # one sweep to size the sample
+    one = time.perf_counter() - t0
+    n = max(1, int(target_s / max(one, 1e-6)))
+    t0 = time.perf_counter()
+    O.run(a, b, radius, O.JACOBI, n, threads)
+    dt = time.perf_counter() - t0
+    return {"value": round(updates(dim, radius, n) / dt / 1e9, 4), "unit": "GCell-updates/s",
+            "cores": threads, "kind": "port",
+            "sample": "%d sweeps of %d^3 R=%d Jacobi (oracle, OpenMP %d threads, %.1f s)"
+                      % (n, dim, radius, threads, dt)}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+    from oracle import oracle as O
+    shape = (args.dim,) * 3
+    u = O.uniform(shape, SEED)
+    threads = os.cpu_count() or 1
+    # each step: a bounded sample of the workload (a few sweeps of the full grid)
+    a, b = u.copy(), u.copy()
+    t0 = time.perf_counter()
+    O.sweep(a, b, args.radius, O.JACOBI, threads)
+    one = time.perf_counter() - t0
+    per_step = max(1, int(8.0 / max(one, 1e-6)))
+    for _ in range(args.warmup):
+        O.sweep(a, b, args.radius, O.JACOBI, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.run(a, b, args.radius, O.JACOBI, per_step, threads)
+    dt = time.perf_counter() - t0
+    value = updates(args.dim, args.radius, per_step) * args.steps / dt / 1e9
+    out = {
+        "impl": "reference",
+        "metric": "GCell-updates/s (3D 512^3 FP32 star stencil, Jacobi, 1000 sweeps)",
+        "value": round(value, 4),
+        "unit": "GCell-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(dt / args.steps * 1e3, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic: border and interior i.i.d. uniform [0,1) (SplitMix64, seed %d)" % SEED,
+        "config": {"workload": "3D %d^3 FP32 star stencil R=%d, Jacobi, %d sweeps per step"
+                               % (args.dim, args.radius, args.sweeps),
+                   "dims": 3, "dim": args.dim, "radius": args.radius, "sweeps": args.sweeps},
+        "cpu_baseline": {"value": round(value, 4), "unit": "GCell-updates/s", "cores": threads,
+                         "kind": "port",
+                         "sample": "%d sweeps per step of %d^3 R=%d (oracle restatement of "
+                                   "src/stencil_cpu.cu, OpenMP %d threads)"
+                                   % (per_step, args.dim, args.radius, threads)},
+        "e2e": {"value": round(value, 4), "unit": "GCell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,188 @@
+/*
+ * stencil_dispatch.h -- C ABI of libstencil_gb300.so, the GB300 (sm_103a)
+ * iterative star-stencil sweep library.
+ *
+ * Plain C: no C++ or CUDA types cross the boundary.  A stream is passed as
+ * stencil_stream_t, which is ABI-identical to cudaStream_t (NULL = the legacy
+ * default stream).  Every entry point returns STENCIL_OK (0) or a negative
+ * STENCIL_E* status; none of them exits the process.
+ *
+ * Grid layout (same as the reference, src/stencil_kernel_base.cu:14): FP32,
+ * x fastest, idx = i + j*nx + k*nx*ny.  A sweep updates exactly the cells whose
+ * every coordinate lies in [R, N-R) (src/stencil_border_check.cu:6-44) and
+ * never writes any other cell ("the border band").
+ */
+#ifndef STENCIL_DISPATCH_H
+#define STENCIL_DISPATCH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define STENCIL_ABI_VERSION 1
+
+typedef struct CUstream_st *stencil_stream_t;
+
+#if defined(__GNUC__)
+#define STENCIL_API __attribute__((visibility("default")))
+#else
+#define STENCIL_API
+#endif
+
+/* Status codes. */
+enum {
+    STENCIL_OK = 0,
+    STENCIL_EINVAL = -1,       /* bad parameter, shape or pointer alignment */
+    STENCIL_ENOMEM = -2,       /* device or pinned-host allocation failed */
+    STENCIL_ECUDA = -3,        /* a CUDA runtime call failed (see stencil_last_error) */
+    STENCIL_ETIMEOUT = -4,     /* a bounded device-side wait gave up */
+    STENCIL_EUNSUPPORTED = -5, /* valid request that this build cannot serve */
+    STENCIL_ENODEVICE = -6     /* no CUDA device of compute capability 10.3 */
+};
+
+/* Update rule. */
+enum {
+    /* u' = (sum of the 2*D*R axis neighbours)/(float)(2*D*R) - u: the reference
+     * formula (src/stencils.cu:18).  The border band of each buffer is whatever
+     * the caller put there (the reference leaves its second buffer as allocated). */
+    STENCIL_MODE_LEGACY = 0,
+    /* u' = (sum of the 2*D*R axis neighbours)/(float)(2*D*R): Jacobi for the
+     * Laplace-type steady state with fixed Dirichlet borders.  The caller keeps
+     * the border band equal in both buffers (stencil_copy_border). */
+    STENCIL_MODE_JACOBI = 1
+};
+
+/* Kernel family.  The first five name the reference's variants
+ * (src/stencil_dispatch.cu:14-42); all of them produce bit-identical results
+ * because every kernel keeps the reference's per-cell summation order. */
+enum {
+    STENCIL_VARIANT_AUTO = 0,          /* library picks (tuning database, then heuristic) */
+    STENCIL_VARIANT_BASE = 1,          /* one sweep per launch, 128-bit vector loads */
+    STENCIL_VARIANT_SMEM = 2,          /* TMA-staged shared-memory tile with halo */
+    STENCIL_VARIANT_SMEM_PADDED = 3,   /* same kernel as SMEM */
+    STENCIL_VARIANT_SMEM_REGISTER = 4, /* 2.5D stream along the slowest axis */
+    STENCIL_VARIANT_COOP = 5,          /* temporally blocked: several sweeps per HBM pass */
+    STENCIL_VARIANT_CLUSTER = 6        /* whole grid resident in a thread-block cluster */
+};
+
+/* Runtime description of one sweep loop.  Zero in a tuning field means "choose". */
+typedef struct stencil_params {
+    int dims;        /* 2 or 3 */
+    int nx, ny, nz;  /* extents; nz is ignored for dims == 2 */
+    int radius;      /* R >= 1, 2R < every extent */
+    int iterations;  /* sweeps, >= 0 */
+    int mode;        /* STENCIL_MODE_* */
+    int variant;     /* STENCIL_VARIANT_* */
+    int block_x, block_y, block_z; /* thread-block shape hint */
+    int coarsen_x;   /* cells per thread along x (vector kernels use multiples of 4) */
+    int temporal;    /* sweeps per pass for STENCIL_VARIANT_COOP */
+    int reserved[4]; /* must be zero */
+} stencil_params;
+
+/* Fills *p with the reference's compile-time defaults
+ * (3-D, 256^3, R=1, 64 sweeps, LEGACY, AUTO). */
+STENCIL_API int stencil_params_init(stencil_params *p);
+
+/* Validates *p without touching the device. */
+STENCIL_API int stencil_params_check(const stencil_params *p);
+
+/* The sweep loop.  Replaces dispatch_kernels(float*, float*)
+ * (src/stencil_dispatch.cu:138-158) and the never-launched cooperative
+ * dispatch (src/stencil_dispatch.cu:160-177).
+ *   d_u1  device buffer holding the initial state (read, and overwritten as
+ *         ping-pong scratch)
+ *   d_u2  device buffer of the same size (ping-pong scratch; its border band
+ *         is read, never written)
+ * Runs asynchronously on `stream`, allocates nothing, and writes to *d_result
+ * (if non-NULL) which of d_u1 / d_u2 holds the state after the last sweep.
+ * Both buffers must be 16-byte aligned (cudaMalloc gives 256). */
+STENCIL_API int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
+                        stencil_stream_t stream, float **d_result);
+
+/* End to end through host memory, the flow of src/main.cu:33-89: copies h_in
+ * into device buffer 1, fills buffer 2 (LEGACY: zero, like the reference's
+ * fresh cudaMalloc; JACOBI: a copy of h_in, so the border band is equal), runs
+ * the sweeps, copies the final state into h_out and synchronises.  Device
+ * buffers come from a per-device workspace that is kept for later calls and
+ * freed by stencil_release().  *ms (if non-NULL) receives the time between
+ * the start of the upload and the end of the download. */
+STENCIL_API int stencil_run_host(const stencil_params *p, const float *h_in, float *h_out, float *ms);
+
+/* Device-side initial states (same generators as the CPU oracle). */
+/* include/stencil_initializer.h:6-52: outermost layer 1.0f, everything else 0. */
+STENCIL_API int stencil_init_reference(const stencil_params *p, float *d_u, stencil_stream_t stream);
+/* count cells i.i.d. uniform [0,1): value(i) = (mix64(mix64(seed) + G*(i+1)) >> 40) * 2^-24,
+ * mix64 = the SplitMix64 finaliser, G = 0x9E3779B97F4A7C15. */
+STENCIL_API int stencil_init_uniform(float *d_u, size_t count, uint64_t seed, stencil_stream_t stream);
+/* Copies the border band of src into dst (JACOBI set-up). */
+STENCIL_API int stencil_copy_border(const stencil_params *p, const float *d_src, float *d_dst,
+                        stencil_stream_t stream);
+
+/* Relative residual ||b - A u||_2 / ||b||_2 of the steady state that JACOBI
+ * iterates to, (A u)(x) = u(x) - mean of the 2*D*R axis neighbours over the
+ * update region, b = the border contributions; squares summed in FP64 on the
+ * GPU.  Synchronises `stream`. */
+STENCIL_API int stencil_residual(const stencil_params *p, const float *d_u, double *rel_residual,
+                     stencil_stream_t stream);
+
+/* Error reporting. */
+STENCIL_API const char *stencil_strerror(int status);
+/* Text of the last failure on the calling thread (empty if none). */
+STENCIL_API const char *stencil_last_error(void);
+/* Reads and clears the device-side status word that bounded waits set when
+ * they give up (0 = no fault).  Synchronises the device. */
+STENCIL_API int stencil_device_status(int *status);
+
+/* Frees every workspace this library holds on the current device. */
+STENCIL_API int stencil_release(void);
+
+/* Library version and the compute capability it was built for (103). */
+STENCIL_API int stencil_version(int *abi_version, int *sm);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+/* Drop-in for the reference's compile-time configured dispatch: shape, radius,
+ * variant and sweep count come from constants.h exactly as they do for
+ * dispatch_kernels (src/stencil_dispatch.cu:138).  Include constants.h (or pass
+ * the -D macros) before this header. */
+#ifdef STENCIL_CONSTANTS_H
+static inline int stencil_params_from_constants(stencil_params *p)
+{
+    int rc = stencil_params_init(p);
+    if (rc) return rc;
+    p->dims = DIMENSIONS;
+    p->nx = NX; p->ny = NY; p->nz = DIMENSIONS == 3 ? NZ : 1;
+    p->radius = RADIUS;
+    p->iterations = ITERATIONS;
+    p->mode = STENCIL_MODE;
+    p->block_x = HEURISTIC ? 0 : BLOCK_X;
+    p->block_y = HEURISTIC ? 0 : BLOCK_Y;
+    p->block_z = HEURISTIC ? 0 : BLOCK_Z;
+    p->coarsen_x = COARSEN_X;
+    p->temporal = TEMPORAL_T;
+    if (COOP) p->variant = STENCIL_VARIANT_COOP;
+    else if (SMEM && REGISTER) p->variant = STENCIL_VARIANT_SMEM_REGISTER;
+    else if (SMEM && PADDED) p->variant = STENCIL_VARIANT_SMEM_PADDED;
+    else if (SMEM) p->variant = STENCIL_VARIANT_SMEM;
+    else p->variant = STENCIL_VARIANT_BASE;
+    return STENCIL_OK;
+}
+
+/* Same role as dispatch_kernels(d_u1, d_u2) (src/stencil_dispatch.cu:138), plus
+ * a stream, a status and the location of the result. */
+static inline int stencil_dispatch(float *d_u1, float *d_u2, stencil_stream_t stream,
+                                   float **d_result)
+{
+    stencil_params p;
+    int rc = stencil_params_from_constants(&p);
+    if (rc) return rc;
+    return stencil_dispatch_ex(&p, d_u1, d_u2, stream, d_result);
+}
+#endif /* STENCIL_CONSTANTS_H */
+
+#endif /* STENCIL_DISPATCH_H */

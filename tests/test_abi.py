@@ -1,0 +1,123 @@
+"""CPU tests of the C ABI: the library builds, loads, exports every declared
+symbol, and validates parameters without touching a device."""
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import pytest
+
+from thesis_gb300 import lib as L
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_every_declared_symbol_is_exported(stencil_lib):
+    names = L.declared_symbols()
+    assert "stencil_dispatch_ex" in names and "stencil_run_host" in names
+    out = subprocess.run(["nm", "-D", "--defined-only", L.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    for n in names:
+        assert getattr(stencil_lib, n) is not None
+
+
+def test_version(stencil_lib):
+    abi, sm = ctypes.c_int(), ctypes.c_int()
+    assert stencil_lib.stencil_version(ctypes.byref(abi), ctypes.byref(sm)) == 0
+    assert abi.value == 1 and sm.value == 103
+
+
+def test_params_defaults_match_reference_constants(stencil_lib):
+    p = L.StencilParams()
+    assert stencil_lib.stencil_params_init(ctypes.byref(p)) == 0
+    # include/constants.h defaults of the reference: 3-D, DIM 256, R 1, 64 sweeps
+    assert (p.dims, p.nx, p.ny, p.nz, p.radius, p.iterations) == (3, 256, 256, 256, 1, 64)
+    assert p.mode == L.MODE_LEGACY and p.variant == L.VARIANT_AUTO
+
+
+@pytest.mark.parametrize("field,value", [
+    ("dims", 1), ("dims", 4), ("radius", 0), ("nx", 2), ("iterations", -1), ("mode", 7),
+    ("variant", 99), ("block_x", -1), ("coarsen_x", -2),
+])
+def test_params_check_rejects(stencil_lib, field, value):
+    p = L.make_params((16, 16, 16), 1, 4)
+    setattr(p, field, value)
+    assert stencil_lib.stencil_params_check(ctypes.byref(p)) == L.EINVAL
+    assert stencil_lib.stencil_last_error().decode()
+
+
+def test_params_check_rejects_oversized_block_and_reserved(stencil_lib):
+    p = L.make_params((16, 16, 16), 1, 4, block=(64, 32, 1))
+    assert stencil_lib.stencil_params_check(ctypes.byref(p)) == L.EINVAL
+    p = L.make_params((16, 16, 16), 1, 4)
+    p.reserved[2] = 1
+    assert stencil_lib.stencil_params_check(ctypes.byref(p)) == L.EINVAL
+    p = L.make_params((9, 9, 9), 4, 4)  # 2R+1 = 9: smallest legal extent
+    assert stencil_lib.stencil_params_check(ctypes.byref(p)) == 0
+    p = L.make_params((8, 9, 9), 4, 4)
+    assert stencil_lib.stencil_params_check(ctypes.byref(p)) == L.EINVAL
+
+
+def test_dispatch_rejects_bad_pointers_without_device(stencil_lib):
+    p = L.make_params((16, 16), 1, 4)
+    res = ctypes.c_void_p()
+    assert stencil_lib.stencil_dispatch_ex(ctypes.byref(p), None, None, None,
+                                           ctypes.byref(res)) == L.EINVAL
+    assert stencil_lib.stencil_dispatch_ex(ctypes.byref(p), ctypes.c_void_p(4096),
+                                           ctypes.c_void_p(4096), None, None) == L.EINVAL
+    assert stencil_lib.stencil_dispatch_ex(ctypes.byref(p), ctypes.c_void_p(4100),
+                                           ctypes.c_void_p(8192), None, None) == L.EINVAL
+
+
+def test_strerror(stencil_lib):
+    for code in (L.OK, L.EINVAL, L.ENOMEM, L.ECUDA, L.ETIMEOUT, L.EUNSUPPORTED, L.ENODEVICE):
+        assert stencil_lib.stencil_strerror(code)
+    assert b"unknown" in stencil_lib.stencil_strerror(12345)
+
+
+DROPIN = r"""
+#include <stdio.h>
+#include "constants.h"
+#include "stencil_dispatch.h"
+int main(void) {
+    stencil_params p;
+    if (stencil_params_from_constants(&p)) return 1;
+    printf("%d %d %d %d %d %d %d %d %d %d %d\n", p.dims, p.nx, p.ny, p.nz, p.radius,
+           p.iterations, p.mode, p.variant, p.block_x, p.coarsen_x, stencil_params_check(&p));
+    return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("flags,expect", [
+    ([], "3 256 256 256 1 64 0 1 32 4 0"),
+    (["-DDIMENSIONS=2", "-DDIM=512", "-DRADIUS=4", "-DITERATIONS=8", "-DSMEM=true",
+      "-DPADDED=true"], "2 512 512 1 4 8 0 3 32 4 0"),
+    (["-DDIM=128", "-DSMEM=true", "-DREGISTER=true", "-DCOARSEN_X=8"],
+     "3 128 128 128 1 64 0 4 32 8 0"),
+    (["-DCOOP=true", "-DSTENCIL_MODE=STENCIL_MODE_JACOBI", "-DHEURISTIC=true"],
+     "3 256 256 256 1 64 1 5 0 4 0"),
+])
+def test_constants_h_dropin(stencil_lib, flags, expect):
+    """A C caller configured with the reference's -D macros gets the same configuration."""
+    with tempfile.TemporaryDirectory() as tmp:
+        src = os.path.join(tmp, "m.c")
+        exe = os.path.join(tmp, "m")
+        open(src, "w").write(DROPIN)
+        subprocess.run(["gcc", "-std=c99", "-o", exe, src, "-I", os.path.join(ROOT, "include"),
+                        L.LIB_PATH, "-Wl,-rpath," + os.path.dirname(L.LIB_PATH)] + flags,
+                       check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.strip()
+    assert out == expect
+
+
+def test_ngpus_must_be_one():
+    with tempfile.TemporaryDirectory() as tmp:
+        src = os.path.join(tmp, "m.c")
+        open(src, "w").write('#include "constants.h"\nint main(void){return 0;}\n')
+        r = subprocess.run(["gcc", "-DNGPUS=2", "-I", os.path.join(ROOT, "include"), "-c", src,
+                            "-o", os.path.join(tmp, "m.o")], capture_output=True, text=True)
+        assert r.returncode != 0 and "NGPUS" in r.stderr

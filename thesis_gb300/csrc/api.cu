@@ -1,0 +1,378 @@
+// api.cu -- the C ABI of libstencil_gb300 (include/stencil_dispatch.h):
+// parameter validation, variant selection, the sweep loop driver, the
+// host-buffer end-to-end entry point, workspaces and error reporting.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "host.hpp"
+
+namespace st {
+
+// Declared in the kernel translation units.
+int launch_init_uniform(float *u, size_t count, uint64_t seed, cudaStream_t s);
+size_t residual_scratch_bytes();
+int launch_residual(const Geom &g, int dims, const float *u, double *scratch, cudaStream_t s);
+bool stream3d_supported(const Geom &g);
+bool tile_supported(const Geom &g, int dims);
+
+static thread_local char t_err[512];
+
+int fail(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_err, sizeof t_err, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return STENCIL_OK;
+    const int code = e == cudaErrorMemoryAllocation ? STENCIL_ENOMEM
+                     : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+                         ? STENCIL_ENODEVICE
+                         : STENCIL_ECUDA;
+    return fail(code, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+Geom make_geom(const stencil_params &p) {
+    Geom g;
+    g.nx = p.nx;
+    g.ny = p.ny;
+    g.nz = p.dims == 3 ? p.nz : 1;
+    g.radius = p.radius;
+    g.legacy = p.mode == STENCIL_MODE_LEGACY;
+    g.sy = p.nx;
+    g.sz = (long long)p.nx * p.ny;
+    return g;
+}
+
+long long cell_count(const stencil_params &p) {
+    return (long long)p.nx * p.ny * (p.dims == 3 ? p.nz : 1);
+}
+
+int current_device() {
+    int d = 0;
+    cudaGetDevice(&d);
+    return d;
+}
+
+int num_sms() {
+    static int cache[64] = {0};
+    const int d = current_device();
+    if (d >= 0 && d < 64 && cache[d]) return cache[d];
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d) != cudaSuccess || n <= 0)
+        n = 152;
+    if (d >= 0 && d < 64) cache[d] = n;
+    return n;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point, so the
+// library does not link libcuda directly.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                  CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+int make_tensor_map(CUtensorMap *map, const float *base, int rank, const long long *dims,
+                    const int *box) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return fail(STENCIL_ECUDA, "cuTensorMapEncodeTiled is unavailable");
+    cuuint64_t gdim[3], gstride[2];
+    cuuint32_t bdim[3], estride[3] = {1, 1, 1};
+    for (int i = 0; i < rank; ++i) {
+        gdim[i] = (cuuint64_t)dims[i];
+        bdim[i] = (cuuint32_t)box[i];
+    }
+    gstride[0] = (cuuint64_t)dims[0] * 4;
+    if (rank == 3) gstride[1] = (cuuint64_t)dims[0] * dims[1] * 4;
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank,
+                    const_cast<float *>(base), gdim, gstride, bdim, estride,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(STENCIL_EINVAL, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return STENCIL_OK;
+}
+
+// Per-device scratch kept between calls (host-buffer entry, residual).
+struct DeviceWorkspace {
+    float *u[2] = {nullptr, nullptr};
+    size_t grid_bytes = 0;
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+};
+
+static std::mutex g_ws_mu;
+static std::vector<DeviceWorkspace> g_ws(64);
+
+static int ws_grids(int dev, size_t bytes, DeviceWorkspace **out) {
+    DeviceWorkspace &w = g_ws[dev];
+    if (!w.stream) {
+        ST_CUDA(cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking));
+        ST_CUDA(cudaEventCreate(&w.ev[0]));
+        ST_CUDA(cudaEventCreate(&w.ev[1]));
+    }
+    if (w.grid_bytes < bytes) {
+        cudaStreamSynchronize(w.stream);
+        cudaFree(w.u[0]);
+        cudaFree(w.u[1]);
+        w.u[0] = w.u[1] = nullptr;
+        w.grid_bytes = 0;
+        ST_CUDA(cudaMalloc(&w.u[0], bytes));
+        ST_CUDA(cudaMalloc(&w.u[1], bytes));
+        w.grid_bytes = bytes;
+    }
+    *out = &w;
+    return STENCIL_OK;
+}
+
+static int ws_scratch(int dev, size_t bytes, void **out) {
+    DeviceWorkspace &w = g_ws[dev];
+    if (w.scratch_bytes < bytes) {
+        cudaDeviceSynchronize();
+        cudaFree(w.scratch);
+        w.scratch = nullptr;
+        w.scratch_bytes = 0;
+        ST_CUDA(cudaMalloc(&w.scratch, bytes));
+        w.scratch_bytes = bytes;
+    }
+    *out = w.scratch;
+    return STENCIL_OK;
+}
+
+// Variant choice when the caller leaves it to the library.
+static int choose_variant(const stencil_params &p) {
+    const Geom g = make_geom(p);
+    if (p.dims == 3 && stream3d_supported(g)) return STENCIL_VARIANT_SMEM_REGISTER;
+    return STENCIL_VARIANT_BASE;
+}
+
+}  // namespace st
+
+using namespace st;
+
+extern "C" {
+
+int stencil_params_init(stencil_params *p) {
+    if (!p) return fail(STENCIL_EINVAL, "null params");
+    memset(p, 0, sizeof *p);
+    p->dims = 3;
+    p->nx = p->ny = p->nz = 256;
+    p->radius = 1;
+    p->iterations = 64;
+    p->mode = STENCIL_MODE_LEGACY;
+    p->variant = STENCIL_VARIANT_AUTO;
+    return STENCIL_OK;
+}
+
+int stencil_params_check(const stencil_params *p) {
+    if (!p) return fail(STENCIL_EINVAL, "null params");
+    if (p->dims != 2 && p->dims != 3) return fail(STENCIL_EINVAL, "dims must be 2 or 3 (got %d)", p->dims);
+    if (p->radius < 1) return fail(STENCIL_EINVAL, "radius must be >= 1");
+    const int nz = p->dims == 3 ? p->nz : 1;
+    if (p->nx < 1 || p->ny < 1 || nz < 1) return fail(STENCIL_EINVAL, "extents must be positive");
+    if (2 * p->radius >= p->nx || 2 * p->radius >= p->ny || (p->dims == 3 && 2 * p->radius >= p->nz))
+        return fail(STENCIL_EINVAL, "every extent must exceed 2*radius");
+    if ((long long)p->nx * p->ny * nz >= (1LL << 40)) return fail(STENCIL_EINVAL, "grid too large");
+    if (p->iterations < 0) return fail(STENCIL_EINVAL, "iterations must be >= 0");
+    if (p->mode != STENCIL_MODE_LEGACY && p->mode != STENCIL_MODE_JACOBI)
+        return fail(STENCIL_EINVAL, "unknown mode %d", p->mode);
+    if (p->variant < STENCIL_VARIANT_AUTO || p->variant > STENCIL_VARIANT_CLUSTER)
+        return fail(STENCIL_EINVAL, "unknown variant %d", p->variant);
+    if (p->block_x < 0 || p->block_y < 0 || p->block_z < 0 || p->coarsen_x < 0 || p->temporal < 0)
+        return fail(STENCIL_EINVAL, "tuning fields must be >= 0");
+    if ((long long)std::max(p->block_x, 1) * std::max(p->block_y, 1) * std::max(p->block_z, 1) > 1024)
+        return fail(STENCIL_EINVAL, "block shape exceeds 1024 threads");
+    for (int r : p->reserved)
+        if (r) return fail(STENCIL_EINVAL, "reserved fields must be zero");
+    return STENCIL_OK;
+}
+
+int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
+                        stencil_stream_t stream, float **d_result) {
+    int rc = stencil_params_check(p);
+    if (rc) return rc;
+    if (!d_u1 || !d_u2 || d_u1 == d_u2) return fail(STENCIL_EINVAL, "two distinct device buffers are required");
+    if ((reinterpret_cast<uintptr_t>(d_u1) | reinterpret_cast<uintptr_t>(d_u2)) & 15)
+        return fail(STENCIL_EINVAL, "device buffers must be 16-byte aligned");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const Geom g = make_geom(*p);
+    float *cur = d_u1, *nxt = d_u2;
+    if (d_result) *d_result = cur;
+    if (p->iterations == 0) return STENCIL_OK;
+    int variant = p->variant == STENCIL_VARIANT_AUTO ? choose_variant(*p) : p->variant;
+    if (variant == STENCIL_VARIANT_SMEM_REGISTER && !(p->dims == 3 && stream3d_supported(g)))
+        variant = STENCIL_VARIANT_SMEM_PADDED;
+    if ((variant == STENCIL_VARIANT_SMEM || variant == STENCIL_VARIANT_SMEM_PADDED) &&
+        !tile_supported(g, p->dims))
+        variant = STENCIL_VARIANT_BASE;
+    if (variant == STENCIL_VARIANT_COOP || variant == STENCIL_VARIANT_CLUSTER)
+        variant = p->dims == 3 && stream3d_supported(g) ? STENCIL_VARIANT_SMEM_REGISTER
+                                                        : STENCIL_VARIANT_BASE;
+    if (variant == STENCIL_VARIANT_SMEM_REGISTER) {
+        float *res = nullptr;
+        rc = run_stream3d(g, cur, nxt, p->iterations, p->block_x ? 4 * p->block_x : 0,
+                          p->block_y, s, &res);
+        if (rc) return rc;
+        if (d_result) *d_result = res;
+        return STENCIL_OK;
+    }
+    for (int it = 0; it < p->iterations; ++it) {
+        if (variant == STENCIL_VARIANT_BASE)
+            rc = launch_base_sweep(g, p->dims, cur, nxt, p->block_x, p->block_y, p->block_z,
+                                   p->coarsen_x, s);
+        else
+            rc = launch_tile_sweep(g, p->dims, cur, nxt, p->block_x, p->block_y, p->block_z, s);
+        if (rc) return rc;
+        std::swap(cur, nxt);
+    }
+    if (d_result) *d_result = cur;
+    return STENCIL_OK;
+}
+
+int stencil_run_host(const stencil_params *p, const float *h_in, float *h_out, float *ms) {
+    int rc = stencil_params_check(p);
+    if (rc) return rc;
+    if (!h_in || !h_out) return fail(STENCIL_EINVAL, "null host buffer");
+    const size_t bytes = (size_t)cell_count(*p) * sizeof(float);
+    std::lock_guard<std::mutex> lock(g_ws_mu);
+    const int dev = current_device();
+    if (dev < 0 || dev >= 64) return fail(STENCIL_ENODEVICE, "device index out of range");
+    DeviceWorkspace *w = nullptr;
+    rc = ws_grids(dev, bytes, &w);
+    if (rc) return rc;
+    ST_CUDA(cudaEventRecord(w->ev[0], w->stream));
+    ST_CUDA(cudaMemcpyAsync(w->u[0], h_in, bytes, cudaMemcpyHostToDevice, w->stream));
+    if (p->mode == STENCIL_MODE_JACOBI)
+        ST_CUDA(cudaMemcpyAsync(w->u[1], w->u[0], bytes, cudaMemcpyDeviceToDevice, w->stream));
+    else
+        ST_CUDA(cudaMemsetAsync(w->u[1], 0, bytes, w->stream));
+    float *res = nullptr;
+    rc = stencil_dispatch_ex(p, w->u[0], w->u[1], reinterpret_cast<stencil_stream_t>(w->stream),
+                             &res);
+    if (rc) {
+        cudaStreamSynchronize(w->stream);
+        return rc;
+    }
+    ST_CUDA(cudaMemcpyAsync(h_out, res, bytes, cudaMemcpyDeviceToHost, w->stream));
+    ST_CUDA(cudaEventRecord(w->ev[1], w->stream));
+    ST_CUDA(cudaStreamSynchronize(w->stream));
+    if (ms) ST_CUDA(cudaEventElapsedTime(ms, w->ev[0], w->ev[1]));
+    return STENCIL_OK;
+}
+
+int stencil_init_reference(const stencil_params *p, float *d_u, stencil_stream_t stream) {
+    int rc = stencil_params_check(p);
+    if (rc) return rc;
+    if (!d_u) return fail(STENCIL_EINVAL, "null buffer");
+    return launch_init_reference(make_geom(*p), p->dims, d_u, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int stencil_init_uniform(float *d_u, size_t count, uint64_t seed, stencil_stream_t stream) {
+    if (!d_u && count) return fail(STENCIL_EINVAL, "null buffer");
+    return launch_init_uniform(d_u, count, seed, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int stencil_copy_border(const stencil_params *p, const float *d_src, float *d_dst,
+                        stencil_stream_t stream) {
+    int rc = stencil_params_check(p);
+    if (rc) return rc;
+    if (!d_src || !d_dst) return fail(STENCIL_EINVAL, "null buffer");
+    return launch_copy_border(make_geom(*p), p->dims, d_src, d_dst,
+                              reinterpret_cast<cudaStream_t>(stream));
+}
+
+int stencil_residual(const stencil_params *p, const float *d_u, double *rel_residual,
+                     stencil_stream_t stream) {
+    int rc = stencil_params_check(p);
+    if (rc) return rc;
+    if (!d_u || !rel_residual) return fail(STENCIL_EINVAL, "null pointer");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    void *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_ws_mu);
+        const int dev = current_device();
+        rc = ws_scratch(dev, residual_scratch_bytes(), &scratch);
+        if (rc) return rc;
+        rc = launch_residual(make_geom(*p), p->dims, d_u, static_cast<double *>(scratch), s);
+        if (rc) return rc;
+        double sums[2];
+        const size_t off = residual_scratch_bytes() / sizeof(double) - 2;
+        ST_CUDA(cudaMemcpyAsync(sums, static_cast<double *>(scratch) + off, sizeof sums,
+                                cudaMemcpyDeviceToHost, s));
+        ST_CUDA(cudaStreamSynchronize(s));
+        *rel_residual = sums[1] > 0.0 ? sqrt(sums[0]) / sqrt(sums[1]) : sqrt(sums[0]);
+    }
+    return STENCIL_OK;
+}
+
+const char *stencil_strerror(int status) {
+    switch (status) {
+        case STENCIL_OK: return "success";
+        case STENCIL_EINVAL: return "invalid argument";
+        case STENCIL_ENOMEM: return "out of memory";
+        case STENCIL_ECUDA: return "CUDA runtime error";
+        case STENCIL_ETIMEOUT: return "device-side wait timed out";
+        case STENCIL_EUNSUPPORTED: return "unsupported configuration";
+        case STENCIL_ENODEVICE: return "no suitable CUDA device";
+        default: return "unknown status";
+    }
+}
+
+const char *stencil_last_error(void) { return t_err; }
+
+int stencil_device_status(int *status) {
+    if (!status) return fail(STENCIL_EINVAL, "null pointer");
+    ST_CUDA(cudaDeviceSynchronize());
+    unsigned v = 0, zero = 0;
+    ST_CUDA(cudaMemcpyFromSymbol(&v, g_device_status, sizeof v));
+    ST_CUDA(cudaMemcpyToSymbol(g_device_status, &zero, sizeof zero));
+    *status = (int)v;
+    return STENCIL_OK;
+}
+
+int stencil_release(void) {
+    std::lock_guard<std::mutex> lock(g_ws_mu);
+    const int dev = current_device();
+    if (dev < 0 || dev >= 64) return STENCIL_OK;
+    DeviceWorkspace &w = g_ws[dev];
+    if (w.stream) cudaStreamSynchronize(w.stream);
+    cudaFree(w.u[0]);
+    cudaFree(w.u[1]);
+    cudaFree(w.scratch);
+    if (w.ev[0]) cudaEventDestroy(w.ev[0]);
+    if (w.ev[1]) cudaEventDestroy(w.ev[1]);
+    if (w.stream) cudaStreamDestroy(w.stream);
+    w = DeviceWorkspace();
+    return STENCIL_OK;
+}
+
+int stencil_version(int *abi_version, int *sm) {
+    if (abi_version) *abi_version = STENCIL_ABI_VERSION;
+    if (sm) *sm = 103;
+    return STENCIL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,209 @@
+// common.cuh -- shared device helpers of libstencil_gb300: the per-cell star
+// update in the reference's summation order, PTX wrappers for mbarrier / TMA /
+// clusters, and bounded waits that report through a device status word instead
+// of hanging.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/stencil_dispatch.h"
+
+namespace st {
+
+// ---------------------------------------------------------------------------
+// Geometry of one grid as the kernels see it.
+// ---------------------------------------------------------------------------
+struct Geom {
+    int nx, ny, nz;      // nz == 1 for 2-D
+    int radius;
+    int legacy;          // 1: subtract the centre (STENCIL_MODE_LEGACY)
+    long long sy, sz;    // strides of y and z in cells
+};
+
+// Device status word: bounded waits that give up OR in a code and return.
+// Read and cleared by stencil_device_status().
+enum : unsigned { kStatusTimeout = 1u, kStatusBadLaunch = 2u };
+extern __device__ unsigned g_device_status;
+
+__device__ __forceinline__ void report_status(unsigned code) { atomicOr(&g_device_status, code); }
+
+// ---------------------------------------------------------------------------
+// The per-cell update.  Order follows src/stencils.cu:8-19 with
+// src/stencil_accumulators.cu:6-16: axes i, j, k; on each axis the offsets
+// -R..-1 ("prev", distance R down to 1) and then +1..+R ("next").  One float
+// accumulator starting at 0.0f; then acc / (float)(2*D*R) (IEEE division:
+// this library is never built with fast-math) and, in LEGACY mode, minus the
+// centre value.  Every kernel calls this with its own value source, so all
+// variants are bit-identical to the reference.
+// ---------------------------------------------------------------------------
+template <int D, int R, class Get>
+__device__ __forceinline__ float star_sum(Get get) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+#pragma unroll
+        for (int o = -R; o <= R; ++o)
+            if (o != 0) acc += get(a, o);
+    }
+    return acc;
+}
+
+template <int D, int R>
+__device__ __forceinline__ float star_finish(float acc, float centre, int legacy) {
+    constexpr float coeff = (float)(2 * D * R);
+    float v = acc / coeff;
+    return legacy ? v - centre : v;
+}
+
+// Runtime-radius forms for the generic kernels.
+__device__ __forceinline__ float star_finish_rt(float acc, float coeff, float centre,
+                                                int legacy) {
+    float v = acc / coeff;
+    return legacy ? v - centre : v;
+}
+
+// ---------------------------------------------------------------------------
+// PTX wrappers.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Default limit of one bounded wait: 2 s.  A healthy wait in these kernels
+// ends in microseconds.
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+
+// Waits for the phase with the given parity of an mbarrier.  Returns false
+// (after setting the device status word) if the limit passes first.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    while (!mbar_try_wait(bar, parity)) {
+        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+            report_status(kStatusTimeout);
+            return false;
+        }
+    }
+    return true;
+}
+
+// TMA tiled loads into this CTA's shared memory, completion on an mbarrier.
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar,
+                                            int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar,
+                                            int x, int y, int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+        : "memory");
+}
+
+__device__ __forceinline__ void prefetch_tensormap(const CUtensorMap *map) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+// Thread-block cluster helpers.
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t cluster_nctarank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ void cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+                 "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Address of the same shared-memory variable in CTA `rank` of this cluster.
+__device__ __forceinline__ uint32_t mapa_shared(uint32_t addr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
+}
+
+__device__ __forceinline__ void st_cluster_f32(uint32_t addr, float v) {
+    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
+}
+
+__device__ __forceinline__ void st_cluster_v4(uint32_t addr, float4 v) {
+    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(v.x),
+                 "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
+
+__device__ __forceinline__ float4 ld_cluster_v4(uint32_t addr) {
+    float4 v;
+    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(addr)
+                 : "memory");
+    return v;
+}
+
+__device__ __forceinline__ float ld_cluster_f32(uint32_t addr) {
+    float v;
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ float f4get(const float4 &v, int c) {
+    return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
+}
+
+// Whether cell coordinate q lies in [R, n-R).
+__device__ __forceinline__ bool in_range(int q, int n, int r) { return q >= r && q < n - r; }
+
+}  // namespace st

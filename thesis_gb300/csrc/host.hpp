@@ -1,0 +1,53 @@
+// host.hpp -- host-side internals shared by the translation units of
+// libstencil_gb300 (not part of the C ABI).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/stencil_dispatch.h"
+#include "common.cuh"
+
+namespace st {
+
+// Records a failure for stencil_last_error() and returns `code`.
+int fail(int code, const char *fmt, ...);
+// Maps a CUDA runtime error to STENCIL_ECUDA (recording the message) or OK.
+int cuda_fail(cudaError_t e, const char *what);
+#define ST_CUDA(call)                                             \
+    do {                                                          \
+        cudaError_t st_e_ = (call);                               \
+        if (st_e_ != cudaSuccess) return ::st::cuda_fail(st_e_, #call); \
+    } while (0)
+
+Geom make_geom(const stencil_params &p);
+long long cell_count(const stencil_params &p);
+int num_sms();
+int current_device();
+
+// Builds a tiled TMA descriptor for an FP32 grid (rank 2 or 3).
+int make_tensor_map(CUtensorMap *map, const float *base, int rank, const long long *dims,
+                    const int *box);
+
+// One sweep per launch kernels (src -> dst).  Each returns a status.
+int launch_base_sweep(const Geom &g, int dims, const float *src, float *dst, int bx, int by,
+                      int bz, int cf, cudaStream_t s);
+int launch_tile_sweep(const Geom &g, int dims, const float *src, float *dst, int bx, int by,
+                      int bz, cudaStream_t s);
+
+// Multi-sweep drivers: run `iters` sweeps ping-ponging between a and b
+// starting from a; *res receives the buffer holding the final state.
+int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int tile_y,
+                 cudaStream_t s, float **res);
+int run_tb3d(const Geom &g, float *a, float *b, int iters, int temporal, cudaStream_t s,
+             float **res);
+int run_cluster2d(const Geom &g, float *a, float *b, int iters, cudaStream_t s, float **res);
+bool cluster2d_fits(const Geom &g);
+
+// Plain whole-grid helpers.
+int launch_copy_border(const Geom &g, int dims, const float *src, float *dst, cudaStream_t s);
+int launch_init_reference(const Geom &g, int dims, float *u, cudaStream_t s);
+
+}  // namespace st

@@ -1,0 +1,173 @@
+// k_util.cu -- whole-grid helper kernels: seeded initial states, border copy,
+// and the FP64 residual norm.
+#include <algorithm>
+
+#include "host.hpp"
+
+namespace st {
+
+__device__ unsigned g_device_status = 0;
+
+// SplitMix64 finaliser (Steele, Lea & Flood 2014); identical to the oracle's.
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void k_init_uniform(float *__restrict__ u, size_t count, uint64_t seed) {
+    const uint64_t base = mix64(seed);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const uint64_t z = mix64(base + 0x9E3779B97F4A7C15ull * (i + 1));
+        u[i] = (float)(z >> 40) * (1.0f / 16777216.0f);
+    }
+}
+
+// include/stencil_initializer.h:6-52: outermost layer 1, else 0.
+__global__ void k_init_reference(float *__restrict__ u, Geom g, int dims) {
+    const size_t n = (size_t)g.nx * g.ny * (dims == 3 ? g.nz : 1);
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(idx % g.nx);
+        const int j = (int)((idx / g.nx) % g.ny);
+        const int k = (int)(idx / ((size_t)g.nx * g.ny));
+        const bool edge = i == 0 || i == g.nx - 1 || j == 0 || j == g.ny - 1 ||
+                          (dims == 3 && (k == 0 || k == g.nz - 1));
+        u[idx] = edge ? 1.0f : 0.0f;
+    }
+}
+
+// Copies cells outside the update region.  One thread per (row, plane) walks
+// the row's border cells; rows outside the update region are copied whole.
+__global__ void k_copy_border(const float *__restrict__ src, float *__restrict__ dst, Geom g,
+                              int dims) {
+    const int R = g.radius;
+    const long long rows = (long long)g.ny * (dims == 3 ? g.nz : 1);
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int j = (int)(r % g.ny), k = (int)(r / g.ny);
+        const long long base = (long long)j * g.sy + (long long)k * g.sz;
+        const bool whole = !in_range(j, g.ny, R) || (dims == 3 && !in_range(k, g.nz, R));
+        if (whole) {
+            for (int i = threadIdx.x; i < g.nx; i += blockDim.x) dst[base + i] = src[base + i];
+        } else {
+            for (int i = threadIdx.x; i < 2 * R; i += blockDim.x) {
+                const int x = i < R ? i : g.nx - 2 * R + i;
+                dst[base + x] = src[base + x];
+            }
+        }
+    }
+}
+
+// Residual of the JACOBI steady state, accumulated in FP64: per update-region
+// cell r = (sum of neighbours)/(2DR) - u, b = (sum of border neighbours)/(2DR).
+// Stage 1 writes one (sum r^2, sum b^2) pair per block; stage 2 adds the pairs
+// in a fixed order, so the result does not depend on scheduling.
+constexpr int kResidBlocks = 1024;
+constexpr int kResidThreads = 256;
+
+__device__ __forceinline__ void block_sum2(double &a, double &b, double *sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { sh[2 * w] = a; sh[2 * w + 1] = b; }
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        a = l < nw ? sh[2 * l] : 0.0;
+        b = l < nw ? sh[2 * l + 1] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, o);
+            b += __shfl_down_sync(0xffffffffu, b, o);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kResidThreads)
+    k_residual_partial(const float *__restrict__ u, Geom g, int dims, double *__restrict__ part) {
+    __shared__ double sh[2 * (kResidThreads / 32)];
+    const int R = g.radius;
+    const int ix = g.nx - 2 * R, iy = g.ny - 2 * R, iz = dims == 3 ? g.nz - 2 * R : 1;
+    const long long n = (long long)ix * iy * iz;
+    const double coeff = 2.0 * dims * R;
+    double rr = 0.0, bb = 0.0;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = R + (int)(c % ix);
+        const int j = R + (int)((c / ix) % iy);
+        const int k = dims == 3 ? R + (int)(c / ((long long)ix * iy)) : 0;
+        const long long idx = i + (long long)j * g.sy + (long long)k * g.sz;
+        double all = 0.0, bnd = 0.0;
+        for (int o = -R; o <= R; ++o) {
+            if (!o) continue;
+            const double v = u[idx + o];
+            all += v;
+            if (!in_range(i + o, g.nx, R)) bnd += v;
+        }
+        for (int o = -R; o <= R; ++o) {
+            if (!o) continue;
+            const double v = u[idx + o * g.sy];
+            all += v;
+            if (!in_range(j + o, g.ny, R)) bnd += v;
+        }
+        if (dims == 3)
+            for (int o = -R; o <= R; ++o) {
+                if (!o) continue;
+                const double v = u[idx + o * g.sz];
+                all += v;
+                if (!in_range(k + o, g.nz, R)) bnd += v;
+            }
+        const double r = all / coeff - (double)u[idx];
+        bnd /= coeff;
+        rr += r * r;
+        bb += bnd * bnd;
+    }
+    block_sum2(rr, bb, sh);
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = rr; part[2 * blockIdx.x + 1] = bb; }
+}
+
+__global__ void __launch_bounds__(kResidThreads)
+    k_residual_final(const double *__restrict__ part, int nparts, double *__restrict__ out) {
+    __shared__ double sh[2 * (kResidThreads / 32)];
+    double rr = 0.0, bb = 0.0;
+    for (int p = threadIdx.x; p < nparts; p += blockDim.x) {
+        rr += part[2 * p];
+        bb += part[2 * p + 1];
+    }
+    block_sum2(rr, bb, sh);
+    if (threadIdx.x == 0) { out[0] = rr; out[1] = bb; }
+}
+
+int launch_init_reference(const Geom &g, int dims, float *u, cudaStream_t s) {
+    k_init_reference<<<4 * num_sms(), 256, 0, s>>>(u, g, dims);
+    return cuda_fail(cudaGetLastError(), "init_reference launch");
+}
+
+int launch_copy_border(const Geom &g, int dims, const float *src, float *dst, cudaStream_t s) {
+    k_copy_border<<<8 * num_sms(), 128, 0, s>>>(src, dst, g, dims);
+    return cuda_fail(cudaGetLastError(), "copy_border launch");
+}
+
+int launch_init_uniform(float *u, size_t count, uint64_t seed, cudaStream_t s) {
+    if (!count) return STENCIL_OK;
+    const int blocks = (int)std::min<size_t>((count + 255) / 256, 8 * (size_t)num_sms());
+    k_init_uniform<<<blocks, 256, 0, s>>>(u, count, seed);
+    return cuda_fail(cudaGetLastError(), "init_uniform launch");
+}
+
+// scratch: >= residual_scratch_bytes() of device memory, 8-byte aligned.
+size_t residual_scratch_bytes() { return (2 * kResidBlocks + 2) * sizeof(double); }
+
+int launch_residual(const Geom &g, int dims, const float *u, double *scratch, cudaStream_t s) {
+    k_residual_partial<<<kResidBlocks, kResidThreads, 0, s>>>(u, g, dims, scratch);
+    ST_CUDA(cudaGetLastError());
+    k_residual_final<<<1, kResidThreads, 0, s>>>(scratch, kResidBlocks,
+                                                  scratch + 2 * kResidBlocks);
+    return cuda_fail(cudaGetLastError(), "residual launch");
+}
+
+}  // namespace st

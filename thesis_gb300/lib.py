@@ -1,0 +1,123 @@
+"""ctypes binding of libstencil_gb300.so (the C ABI in include/stencil_dispatch.h).
+
+The library is the in-tree build next to this file; importing this module
+never falls back to anything else: if the shared library is missing or fails
+to load, ``load()`` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libstencil_gb300.so")
+HEADER_DIR = os.path.join(os.path.dirname(HERE), "include")
+
+OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, EUNSUPPORTED, ENODEVICE = 0, -1, -2, -3, -4, -5, -6
+MODE_LEGACY, MODE_JACOBI = 0, 1
+VARIANT_AUTO, VARIANT_BASE, VARIANT_SMEM, VARIANT_SMEM_PADDED = 0, 1, 2, 3
+VARIANT_SMEM_REGISTER, VARIANT_COOP, VARIANT_CLUSTER = 4, 5, 6
+VARIANT_NAMES = {
+    "auto": VARIANT_AUTO, "base": VARIANT_BASE, "smem": VARIANT_SMEM,
+    "smem_padded": VARIANT_SMEM_PADDED, "smem_register": VARIANT_SMEM_REGISTER,
+    "coop": VARIANT_COOP, "cluster": VARIANT_CLUSTER,
+}
+
+
+class StencilError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str = ""):
+        self.status = status
+        msg = "%s failed: %s (%d)" % (where, _strerror(status), status)
+        if detail:
+            msg += ": " + detail
+        super().__init__(msg)
+
+
+class StencilParams(ctypes.Structure):
+    _fields_ = [
+        ("dims", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+        ("nz", ctypes.c_int), ("radius", ctypes.c_int), ("iterations", ctypes.c_int),
+        ("mode", ctypes.c_int), ("variant", ctypes.c_int), ("block_x", ctypes.c_int),
+        ("block_y", ctypes.c_int), ("block_z", ctypes.c_int), ("coarsen_x", ctypes.c_int),
+        ("temporal", ctypes.c_int), ("reserved", ctypes.c_int * 4),
+    ]
+
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    """Loads the in-tree library (raises if it is absent: there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libstencil_gb300.so is not built (run __graft_entry__.build())")
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.POINTER(StencilParams)
+    vp, i, sz, u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_uint64
+    sig = {
+        "stencil_params_init": (i, [P]),
+        "stencil_params_check": (i, [P]),
+        "stencil_dispatch_ex": (i, [P, vp, vp, vp, ctypes.POINTER(vp)]),
+        "stencil_run_host": (i, [P, vp, vp, ctypes.POINTER(ctypes.c_float)]),
+        "stencil_init_reference": (i, [P, vp, vp]),
+        "stencil_init_uniform": (i, [vp, sz, u64, vp]),
+        "stencil_copy_border": (i, [P, vp, vp, vp]),
+        "stencil_residual": (i, [P, vp, ctypes.POINTER(ctypes.c_double), vp]),
+        "stencil_strerror": (ctypes.c_char_p, [i]),
+        "stencil_last_error": (ctypes.c_char_p, []),
+        "stencil_device_status": (i, [ctypes.POINTER(i)]),
+        "stencil_release": (i, []),
+        "stencil_version": (i, [ctypes.POINTER(i), ctypes.POINTER(i)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _strerror(status: int) -> str:
+    try:
+        return load().stencil_strerror(status).decode()
+    except Exception:  # pragma: no cover - only when the library itself is missing
+        return "status %d" % status
+
+
+def check(status: int, where: str) -> None:
+    if status != OK:
+        raise StencilError(status, where, load().stencil_last_error().decode())
+
+
+def declared_symbols() -> list[str]:
+    """Every function include/*.h declares with STENCIL_API / UNET_API."""
+    names = []
+    for fn in sorted(os.listdir(HEADER_DIR)):
+        if not fn.endswith(".h"):
+            continue
+        text = "\n".join(line for line in open(os.path.join(HEADER_DIR, fn))
+                         if not line.lstrip().startswith("#"))
+        names += re.findall(r"\b(?:STENCIL_API|UNET_API)\s+[\w\s\*]*?\b(\w+)\s*\(", text)
+    return names
+
+
+def make_params(shape, radius: int, iterations: int, mode: int = MODE_LEGACY,
+                variant: int = VARIANT_AUTO, block=(0, 0, 0), coarsen_x: int = 0,
+                temporal: int = 0) -> StencilParams:
+    """shape is numpy/torch order: (ny, nx) for 2-D, (nz, ny, nx) for 3-D."""
+    p = StencilParams()
+    check(load().stencil_params_init(ctypes.byref(p)), "stencil_params_init")
+    if len(shape) == 2:
+        p.dims, p.ny, p.nx, p.nz = 2, shape[0], shape[1], 1
+    elif len(shape) == 3:
+        p.dims, p.nz, p.ny, p.nx = 3, shape[0], shape[1], shape[2]
+    else:
+        raise ValueError("grid must be 2-D or 3-D")
+    p.radius, p.iterations, p.mode = radius, iterations, mode
+    p.variant = VARIANT_NAMES[variant] if isinstance(variant, str) else variant
+    p.block_x, p.block_y, p.block_z = block
+    p.coarsen_x, p.temporal = coarsen_x, temporal
+    return p

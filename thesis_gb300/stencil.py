@@ -1,0 +1,159 @@
+"""Host-side interface of the sweep loop, mirroring the reference's dispatch.
+
+The reference configures one binary per configuration with the compile-time
+macros of include/constants.h and runs ``dispatch_kernels(d_u1, d_u2)``
+(src/stencil_dispatch.cu:138-158).  ``StencilConfig`` keeps those macro names
+as fields, and ``dispatch_kernels`` takes the same two device buffers; both go
+straight to the C ABI (``stencil_dispatch_ex``).  Device memory is held in
+torch CUDA tensors (plumbing only: every sweep runs in libstencil_gb300.so).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import lib as _lib
+
+
+@dataclass
+class StencilConfig:
+    """Runtime form of include/constants.h (same names and defaults)."""
+    DIMENSIONS: int = 3
+    DIM: int = 256
+    RADIUS: int = 1
+    ITERATIONS: int = 64
+    BLOCK_X: int = 32
+    BLOCK_Y: int = 2
+    BLOCK_Z: int = 2
+    COARSEN_X: int = 4
+    SMEM: bool = False
+    PADDED: bool = False
+    REGISTER: bool = False
+    COOP: bool = False
+    HEURISTIC: bool = False
+    STENCIL_MODE: int = _lib.MODE_LEGACY
+    TEMPORAL_T: int = 0
+
+    @property
+    def shape(self):
+        return (self.DIM,) * self.DIMENSIONS
+
+    def variant(self) -> int:
+        """Variant selection of get_kernel() (src/stencil_dispatch.cu:14-42)."""
+        if self.COOP:
+            return _lib.VARIANT_COOP
+        if self.SMEM and self.REGISTER:
+            return _lib.VARIANT_SMEM_REGISTER
+        if self.SMEM and self.PADDED:
+            return _lib.VARIANT_SMEM_PADDED
+        if self.SMEM:
+            return _lib.VARIANT_SMEM
+        return _lib.VARIANT_BASE
+
+    def params(self) -> _lib.StencilParams:
+        block = (0, 0, 0) if self.HEURISTIC else (self.BLOCK_X, self.BLOCK_Y, self.BLOCK_Z)
+        return _lib.make_params(self.shape, self.RADIUS, self.ITERATIONS, self.STENCIL_MODE,
+                                self.variant(), block, self.COARSEN_X, self.TEMPORAL_T)
+
+
+def _stream_handle(stream):
+    import torch
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def _check_tensor(t, shape=None):
+    import torch
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError("device buffers must be CUDA tensors")
+    if t.dtype != torch.float32 or not t.is_contiguous():
+        raise TypeError("device buffers must be contiguous float32")
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise ValueError("buffer shape %s does not match %s" % (tuple(t.shape), tuple(shape)))
+
+
+def dispatch(params: _lib.StencilParams, d_u1, d_u2, stream=None):
+    """Runs params.iterations sweeps; returns whichever of d_u1 / d_u2 holds the result."""
+    _check_tensor(d_u1)
+    _check_tensor(d_u2, d_u1.shape)
+    res = ctypes.c_void_p()
+    _lib.check(_lib.load().stencil_dispatch_ex(ctypes.byref(params), ctypes.c_void_p(d_u1.data_ptr()),
+                                               ctypes.c_void_p(d_u2.data_ptr()),
+                                               _stream_handle(stream), ctypes.byref(res)),
+               "stencil_dispatch_ex")
+    return d_u1 if res.value == d_u1.data_ptr() else d_u2
+
+
+def dispatch_kernels(d_u1, d_u2, cfg: StencilConfig | None = None, stream=None):
+    """Same role as the reference's dispatch_kernels(d_u1, d_u2); returns the result buffer."""
+    cfg = cfg or StencilConfig()
+    return dispatch(cfg.params(), d_u1, d_u2, stream)
+
+
+def sweep(d_u1, d_u2, radius: int, iterations: int, mode: int = _lib.MODE_JACOBI,
+          variant="auto", block=(0, 0, 0), coarsen_x: int = 0, temporal: int = 0, stream=None):
+    p = _lib.make_params(tuple(d_u1.shape), radius, iterations, mode, variant, block,
+                         coarsen_x, temporal)
+    return dispatch(p, d_u1, d_u2, stream)
+
+
+def init_reference(shape, device="cuda", stream=None):
+    import torch
+    u = torch.empty(shape, dtype=torch.float32, device=device)
+    p = _lib.make_params(shape, 1, 0)
+    _lib.check(_lib.load().stencil_init_reference(ctypes.byref(p), ctypes.c_void_p(u.data_ptr()),
+                                                  _stream_handle(stream)), "stencil_init_reference")
+    return u
+
+
+def init_uniform(shape, seed: int, device="cuda", stream=None):
+    import torch
+    u = torch.empty(shape, dtype=torch.float32, device=device)
+    _lib.check(_lib.load().stencil_init_uniform(ctypes.c_void_p(u.data_ptr()), u.numel(),
+                                                seed, _stream_handle(stream)),
+               "stencil_init_uniform")
+    return u
+
+
+def copy_border(src, dst, radius: int, stream=None):
+    _check_tensor(src)
+    _check_tensor(dst, src.shape)
+    p = _lib.make_params(tuple(src.shape), radius, 0)
+    _lib.check(_lib.load().stencil_copy_border(ctypes.byref(p), ctypes.c_void_p(src.data_ptr()),
+                                               ctypes.c_void_p(dst.data_ptr()),
+                                               _stream_handle(stream)), "stencil_copy_border")
+
+
+def residual(u, radius: int, stream=None) -> float:
+    _check_tensor(u)
+    p = _lib.make_params(tuple(u.shape), radius, 0)
+    out = ctypes.c_double()
+    _lib.check(_lib.load().stencil_residual(ctypes.byref(p), ctypes.c_void_p(u.data_ptr()),
+                                            ctypes.byref(out), _stream_handle(stream)),
+               "stencil_residual")
+    return out.value
+
+
+def run_host(h_in: np.ndarray, radius: int, iterations: int, mode: int = _lib.MODE_JACOBI,
+             variant="auto", block=(0, 0, 0), coarsen_x: int = 0, temporal: int = 0,
+             out: np.ndarray | None = None):
+    """End to end from host memory (stencil_run_host); returns (result, ms)."""
+    h_in = np.ascontiguousarray(h_in, dtype=np.float32)
+    if out is None:
+        out = np.empty_like(h_in)
+    p = _lib.make_params(h_in.shape, radius, iterations, mode, variant, block, coarsen_x,
+                         temporal)
+    ms = ctypes.c_float()
+    _lib.check(_lib.load().stencil_run_host(ctypes.byref(p), ctypes.c_void_p(h_in.ctypes.data),
+                                            ctypes.c_void_p(out.ctypes.data), ctypes.byref(ms)),
+               "stencil_run_host")
+    return out, ms.value
+
+
+def device_status() -> int:
+    st = ctypes.c_int()
+    _lib.check(_lib.load().stencil_device_status(ctypes.byref(st)), "stencil_device_status")
+    return st.value
