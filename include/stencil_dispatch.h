@@ -128,6 +128,20 @@ STENCIL_API int stencil_copy_border(const stencil_params *p, const float *d_src,
 STENCIL_API int stencil_residual(const stencil_params *p, const float *d_u, double *rel_residual,
                      stencil_stream_t stream);
 
+/* Same result as stencil_residual, for callers that must not allocate device
+ * memory -- e.g. a process whose own pool allocator already owns all free
+ * device memory, or a latency-critical loop where cudaMalloc/cudaFree and
+ * their device-wide synchronisation are not allowed.  No counterpart in the
+ * reference.  Allocates nothing: its scratch is a fixed 262,160-byte device
+ * array inside the library (kept on every GPU that loads it until exit), so
+ * grids with more than 2^30 update cells are rejected with STENCIL_EINVAL.
+ * The first call on each device looks up that array's address; make it before
+ * any stream capture begins.  Calls share the array: calls that can overlap on
+ * one GPU (two streams, two host threads) race and must be serialised.
+ * Synchronises `stream`. */
+STENCIL_API int stencil_residual_noalloc(const stencil_params *p, const float *d_u,
+                                         double *rel_residual, stencil_stream_t stream);
+
 /* Error reporting. */
 STENCIL_API const char *stencil_strerror(int status);
 /* Text of the last failure on the calling thread (empty if none). */

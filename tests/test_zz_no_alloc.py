@@ -1,0 +1,69 @@
+"""stencil_residual_noalloc: the residual norm for callers that cannot allocate.
+
+Such callers -- a process whose pool allocator already owns all free device
+memory, or a latency-critical loop where cudaMalloc/cudaFree and their
+device-wide synchronisation are not allowed -- get the same answer as
+stencil_residual without the library allocating anything: the scratch lives in
+a fixed device array inside the library.  This file is named so that pytest
+collects it last.
+"""
+import ctypes
+
+import pytest
+
+from thesis_gb300 import lib as L
+
+
+def _noalloc(p, u):
+    out = ctypes.c_double()
+    rc = L.load().stencil_residual_noalloc(ctypes.byref(p), ctypes.c_void_p(u.data_ptr()),
+                                           ctypes.byref(out), None)
+    L.check(rc, "stencil_residual_noalloc")
+    return out.value
+
+
+def _regular(p, u):
+    out = ctypes.c_double()
+    rc = L.load().stencil_residual(ctypes.byref(p), ctypes.c_void_p(u.data_ptr()),
+                                   ctypes.byref(out), None)
+    L.check(rc, "stencil_residual")
+    return out.value
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape,radius", [((96, 80), 1), ((30, 40, 50), 2), ((512, 512), 4),
+                                          ((160, 128, 136), 1)])
+def test_noalloc_matches_regular_entry_point(cuda, shape, radius):
+    """Two calls in a row through the C ABI agree with stencil_residual (rel 1e-12)."""
+    from thesis_gb300 import stencil as S
+    u = S.init_uniform(shape, 4242)
+    p = L.make_params(shape, radius, 0)
+    want = _regular(p, u)
+    first = _noalloc(p, u)
+    second = _noalloc(p, u)
+    assert first == pytest.approx(want, rel=1e-12)
+    assert second == pytest.approx(want, rel=1e-12)
+
+
+@pytest.mark.gpu
+def test_noalloc_leftover_contents_do_not_leak(cuda):
+    """A large call followed by a small one: the small one reads only its own sums."""
+    from thesis_gb300 import stencil as S
+    big = S.init_uniform((200, 200, 200), 1)
+    small = S.init_uniform((40, 40), 2)
+    pb, ps = L.make_params(tuple(big.shape), 1, 0), L.make_params(tuple(small.shape), 1, 0)
+    _noalloc(pb, big)
+    assert _noalloc(ps, small) == pytest.approx(_regular(ps, small), rel=1e-12)
+
+
+def test_noalloc_rejects_grids_beyond_its_fixed_scratch(stencil_lib):
+    """More than 2^30 update cells needs more partial sums than the fixed array holds;
+    the call is refused before anything reaches the device."""
+    p = L.make_params((1026, 1026, 1026), 1, 0)  # 1024^3 = 2^30 update cells: fits
+    q = L.make_params((1027, 1026, 1026), 1, 0)  # one plane more: does not
+    out = ctypes.c_double()
+    rc = stencil_lib.stencil_residual_noalloc(ctypes.byref(q), ctypes.c_void_p(4096),
+                                              ctypes.byref(out), None)
+    assert rc == L.EINVAL
+    assert b"at most" in stencil_lib.stencil_last_error()
+    assert stencil_lib.stencil_params_check(ctypes.byref(p)) == L.OK

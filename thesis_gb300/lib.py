@@ -66,6 +66,7 @@ def load() -> ctypes.CDLL:
         "stencil_init_uniform": (i, [vp, sz, u64, vp]),
         "stencil_copy_border": (i, [P, vp, vp, vp]),
         "stencil_residual": (i, [P, vp, ctypes.POINTER(ctypes.c_double), vp]),
+        "stencil_residual_noalloc": (i, [P, vp, ctypes.POINTER(ctypes.c_double), vp]),
         "stencil_strerror": (ctypes.c_char_p, [i]),
         "stencil_last_error": (ctypes.c_char_p, []),
         "stencil_device_status": (i, [ctypes.POINTER(i)]),
