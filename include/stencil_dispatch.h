@@ -150,6 +150,19 @@ STENCIL_API const char *stencil_last_error(void);
  * they give up (0 = no fault).  Synchronises the device. */
 STENCIL_API int stencil_device_status(int *status);
 
+/* Diagnostics (no counterpart in the reference).
+ * stencil_selftest_div: runs the kernels' division-by-coefficient path against
+ * IEEE division for all 2^32 float bit patterns; *mismatches receives the
+ * count (0 expected), *first_mismatch (optional) the smallest failing pattern.
+ * coeff is one of the coefficients 2*D*R the kernels use: 4, 6, 8, 12, 16, 18,
+ * 24, 32, 36, 48, 64, 96.
+ * stencil_selftest_wait: launches one bounded mbarrier wait that nothing
+ * completes, with a limit of limit_ms (1..2000); *completed receives 0 when the
+ * wait gave up and *status the device status word it set (then cleared). */
+STENCIL_API int stencil_selftest_div(int coeff, unsigned long long *mismatches,
+                                     unsigned *first_mismatch);
+STENCIL_API int stencil_selftest_wait(int limit_ms, int *completed, int *status);
+
 /* Frees every workspace this library holds on the current device. */
 STENCIL_API int stencil_release(void);
 

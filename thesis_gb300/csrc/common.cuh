@@ -33,9 +33,9 @@ __device__ __forceinline__ void report_status(unsigned code) { atomicOr(&g_devic
 // The per-cell update.  Order follows src/stencils.cu:8-19 with
 // src/stencil_accumulators.cu:6-16: axes i, j, k; on each axis the offsets
 // -R..-1 ("prev", distance R down to 1) and then +1..+R ("next").  One float
-// accumulator starting at 0.0f; then acc / (float)(2*D*R) (IEEE division:
-// this library is never built with fast-math) and, in LEGACY mode, minus the
-// centre value.  Every kernel calls this with its own value source, so all
+// accumulator starting at 0.0f; then the correctly rounded acc / (float)(2*D*R)
+// (IEEE semantics: this library is never built with fast-math; see div_coeff)
+// and, in LEGACY mode, minus the centre value.  Every kernel calls this with its own value source, so all
 // variants are bit-identical to the reference.
 // ---------------------------------------------------------------------------
 template <int D, int R, class Get>
@@ -50,10 +50,44 @@ __device__ __forceinline__ float star_sum(Get get) {
     return acc;
 }
 
+// ---------------------------------------------------------------------------
+// Correctly rounded division by the stencil coefficient c = 2*D*R, without
+// the general IEEE division sequence.  Method: Markstein, "Computation of
+// elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990: with rc = RN(1/c), q0 = RN(x*rc) is within one ulp of x/c,
+// the remainder r = x - q0*c is exact in one FMA, and RN(q0 + r*rc) is the
+// correctly rounded quotient.  The steps assume no underflow/overflow, so the
+// method is used for +0 and |x| in [2^-100, 2^120] and the plain division
+// otherwise (-0, tiny, huge and non-finite values).  Powers of two divide exactly by a
+// multiplication.  stencil_selftest_div() checks every float bit pattern
+// against the compiler's IEEE division for each coefficient.
+// ---------------------------------------------------------------------------
+template <int C>
+__device__ __forceinline__ bool div_fast_ok(float x) {
+    const float a = fabsf(x);
+    // +0 is exact on the fast path too (the sums never produce -0: they start
+    // from +0.0f, and +0 + -0 = +0).
+    return (C & (C - 1)) == 0 || __float_as_uint(x) == 0u || (a >= 0x1p-100f && a <= 0x1p+120f);
+}
+
+template <int C>
+__device__ __forceinline__ float div_fast(float x) {
+    constexpr float rc = 1.0f / (float)C;
+    if ((C & (C - 1)) == 0) return x * rc;
+    const float q0 = x * rc;
+    const float r = fmaf(-q0, (float)C, x);
+    return fmaf(r, rc, q0);
+}
+
+// Per-value form: the fast path where it applies, else IEEE division.
+template <int C>
+__device__ __forceinline__ float div_coeff(float x) {
+    return div_fast_ok<C>(x) ? div_fast<C>(x) : x / (float)C;
+}
+
 template <int D, int R>
 __device__ __forceinline__ float star_finish(float acc, float centre, int legacy) {
-    constexpr float coeff = (float)(2 * D * R);
-    float v = acc / coeff;
+    const float v = div_coeff<2 * D * R>(acc);
     return legacy ? v - centre : v;
 }
 
@@ -90,6 +124,10 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
                  : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
@@ -114,11 +152,12 @@ constexpr uint64_t kWaitLimitNs = 2000000000ull;
 
 // Waits for the phase with the given parity of an mbarrier.  Returns false
 // (after setting the device status word) if the limit passes first.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
+                                                  uint64_t limit_ns = kWaitLimitNs) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer_ns();
     while (!mbar_try_wait(bar, parity)) {
-        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+        if (globaltimer_ns() - t0 > limit_ns) {
             report_status(kStatusTimeout);
             return false;
         }

@@ -1,153 +1,232 @@
 // k_stream.cu -- 2.5D streaming sweep for 3-D grids ("smem_register" role,
-// src/stencil_kernel_smem_register.cu:8-62, and "coop" single-sweep role).
+// src/stencil_kernel_smem_register.cu:8-62; it is also the single-sweep engine
+// behind the other 3-D variants).
 //
-// A CTA owns an x-y tile of TX x TY cells and a chunk of z-planes, and marches
-// along z.  Plane tiles including their halo ((TX + 2*RA) x (TY + 2*R) cells,
-// RA = R rounded up to 4 so that every TMA x coordinate is 16-byte aligned)
-// are fetched by TMA (cp.async.bulk.tensor.3d, completion on an mbarrier) into
-// a ring of NS = 2R + 1 + LOOK slots: the 2R+1 planes of the current window
-// plus LOOK planes in flight.  Cells outside the grid arrive as zeros (TMA
-// out-of-bounds fill); they are never used by an updated cell.  Each thread
-// computes four consecutive cells of one row: x-neighbours from 16-byte shared
-// loads of its row, y-neighbours from the rows above and below, z-neighbours
-// from the other planes of the window.  Every input cell is read from HBM
-// once per sweep; halos of neighbouring tiles and chunks come from L2.
+// A CTA owns an x-y tile of TX x TY cells and a chunk of z-planes and marches
+// along z.  Warp-specialised:
+//   * one producer warp (one elected lane) streams plane tiles including their
+//     halo -- (TX + 2*RA) x (TY + 2*R) cells, RA = R rounded up to 4 so every
+//     TMA x coordinate is 16-byte aligned -- into a ring of NS shared-memory
+//     slots with cp.async.bulk.tensor.3d, completion on a per-slot "full"
+//     mbarrier, and refills a slot once every consumer warp has arrived on its
+//     "empty" mbarrier;
+//   * consumer warps compute.  A consumer thread owns 4 consecutive cells of RY
+//     rows.  The z-neighbours of its cells live in a register queue of 2R+1
+//     planes (each plane's own cells are read from shared memory once, when
+//     the plane arrives); x- and y-neighbours come from the centre plane's
+//     slot with 16-byte shared loads.  So a slot is needed only while its
+//     plane is the newest or the centre: the ring holds R+1 planes plus the
+//     planes in flight.
+// Out-of-grid box cells arrive as zeros (TMA out-of-bounds fill) and are never
+// used by an updated cell.  Each input cell is read from HBM once per sweep;
+// halos of neighbouring tiles and chunks are re-read from L2.
 //
-// The work list is (tile, z-chunk) items, chunk-major so that co-resident CTAs
-// work on neighbouring tiles of the same z range (their halo reads hit L2).
-// CTAs loop over items (grid <= resident CTAs) with a monotone plane sequence
-// number that fixes each plane's ring slot and mbarrier parity.
+// Work items are (tile, z-chunk) pairs, chunk-major so that co-resident CTAs
+// work on neighbouring tiles of one z range.  CTAs loop over items; the
+// producer and the consumers walk the same item sequence, and a monotone plane
+// sequence number fixes each plane's slot and mbarrier phase.  No CTA-wide
+// barrier is used after set-up, and every mbarrier wait is bounded.
 #include <algorithm>
 
 #include "host.hpp"
 
 namespace st {
 
-template <int R, int TX, int TY>
+template <int R, int TX, int TY, int RY, int NS>
 struct StreamShape {
     static constexpr int RA = (R + 3) & ~3;
-    static constexpr int PW = TX + 2 * RA;     // plane tile width (cells)
-    static constexpr int PH = TY + 2 * R;      // plane tile height (rows)
+    static constexpr int PW = TX + 2 * RA;  // plane tile width (cells)
+    static constexpr int PH = TY + 2 * R;   // plane tile height (rows)
     static constexpr int PLANE_BYTES = PW * PH * 4;
-    static constexpr int SLOT_BYTES = (PLANE_BYTES + 127) & ~127;
-    static constexpr int LOOK = R >= 4 ? 2 : 3;
-    static constexpr int NS = 2 * R + 1 + LOOK;
-    static constexpr int THREADS = (TX / 4) * TY;
-    // ring + alignment slack + one mbarrier per slot
-    static constexpr int SMEM_BYTES = NS * SLOT_BYTES + 128 + NS * 8;
+    static constexpr int SLOT_FLOATS = ((PLANE_BYTES + 127) & ~127) / 4;
+    static constexpr int CW = TX / 4;       // consumer threads along x
+    static constexpr int CONSUMERS = CW * (TY / RY);
+    static constexpr int CWARPS = CONSUMERS / 32;
+    static constexpr int THREADS = CONSUMERS + 32;
+    static constexpr int SMEM_BYTES = NS * SLOT_FLOATS * 4 + 128 + 2 * NS * 8;
     static_assert(PW <= 256 && PH <= 256, "TMA box dimensions are limited to 256");
-    static_assert(TX % 4 == 0, "TX must be a multiple of 4");
+    static_assert(TX % 4 == 0 && TY % RY == 0 && CONSUMERS % 32 == 0, "bad tile");
+    static_assert((NS & (NS - 1)) == 0 && NS >= R + 2, "ring must be a power of two > R+1");
 };
 
-template <int R, int TX, int TY>
-__global__ void __launch_bounds__(StreamShape<R, TX, TY>::THREADS)
+__device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+
+template <int R, int TX, int TY, int RY, int NS>
+__global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, 1)
     k_stream3d(const __grid_constant__ CUtensorMap src_map, float *__restrict__ dst, Geom g,
                int tiles_x, int tiles_y, int zchunk, int items) {
-    using S = StreamShape<R, TX, TY>;
+    using S = StreamShape<R, TX, TY, RY, NS>;
+    constexpr int C = 6 * R;  // 2*D*R with D = 3
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float *ring = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
                                             ~static_cast<uintptr_t>(127));
-    uint64_t *full = reinterpret_cast<uint64_t *>(ring + S::NS * (S::SLOT_BYTES / 4));
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int tid = tx + ty * (TX / 4);
+    uint64_t *full = reinterpret_cast<uint64_t *>(ring + NS * S::SLOT_FLOATS);
+    uint64_t *empty = full + NS;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         prefetch_tensormap(&src_map);
-        for (int s = 0; s < S::NS; ++s) mbar_init(&full[s], 1);
+        for (int s = 0; s < NS; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], S::CWARPS);
+        }
         fence_mbar_init();
     }
     __syncthreads();
-
-    uint32_t qbase = 0;  // sequence number of the first plane of the current item
     const int ntiles = tiles_x * tiles_y;
+
+    if (warp == S::CWARPS) {
+        // ---------------- producer ----------------
+        if (lane != 0) return;
+        uint32_t q = 0;
+        for (int item = blockIdx.x; item < items; item += gridDim.x) {
+            const int t = item % ntiles, ch = item / ntiles;
+            const int x0 = (t % tiles_x) * TX, y0 = (t / tiles_x) * TY;
+            const int z0 = R + ch * zchunk, z1 = min(z0 + zchunk, g.nz - R);
+            const int np = (z1 - z0) + 2 * R;
+            for (int p = 0; p < np; ++p, ++q) {
+                const int s = q & (NS - 1);
+                const uint32_t use = q / NS;
+                if (use > 0 && !mbar_wait_bounded(&empty[s], (use - 1) & 1)) return;
+                mbar_arrive_expect_tx(&full[s], S::PLANE_BYTES);
+                tma_load_3d(ring + s * S::SLOT_FLOATS, &src_map, &full[s], x0 - S::RA, y0 - R,
+                            z0 - R + p);
+            }
+        }
+        return;
+    }
+
+    // ---------------- consumers ----------------
+    const int cx = tid % S::CW, cy = tid / S::CW;
+    auto release = [&](int s) {
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+    };
+    float4 qz[RY][2 * R + 1];  // z register queue: planes z-R .. z+R of this thread's cells
+    uint32_t qb = 0;           // sequence number of plane 0 of the current item
     for (int item = blockIdx.x; item < items; item += gridDim.x) {
         const int t = item % ntiles, ch = item / ntiles;
         const int x0 = (t % tiles_x) * TX, y0 = (t / tiles_x) * TY;
-        const int z0 = R + ch * zchunk;
-        const int z1 = min(z0 + zchunk, g.nz - R);
-        const int np = (z1 - z0) + 2 * R;  // planes z0-R .. z1+R-1
-        if (tid == 0) {
-            const int pro = min(np, S::NS);
-            for (int p = 0; p < pro; ++p) {
-                const uint32_t q = qbase + p;
-                const int s = q % S::NS;
-                mbar_arrive_expect_tx(&full[s], S::PLANE_BYTES);
-                tma_load_3d(ring + s * (S::SLOT_BYTES / 4), &src_map, &full[s], x0 - S::RA,
-                            y0 - R, z0 - R + p);
-            }
-        }
-        const int x = x0 + 4 * tx, y = y0 + ty;
-        const bool row_live = x < g.nx && in_range(y, g.ny, R);
-        for (int z = z0; z < z1; ++z) {
-            const uint32_t qlo = qbase + (z - z0);  // plane z-R
-            bool ok = true;
-            // Wait for the planes of the window that have not been waited on.
-            for (int p = (z == z0 ? 0 : 2 * R); p <= 2 * R && ok; ++p) {
-                const uint32_t q = qlo + p;
-                ok = mbar_wait_bounded(&full[q % S::NS], (q / S::NS) & 1);
-            }
-            if (ok && row_live) {
-                const float *pl[2 * R + 1];
+        const int z0 = R + ch * zchunk, z1 = min(z0 + zchunk, g.nz - R);
+        const int np = (z1 - z0) + 2 * R;
+        const int x = x0 + 4 * cx, ybase = y0 + cy * RY;
+        const int own = (cy * RY + R) * S::PW + 4 * cx + S::RA;  // slot offset of row 0, cell 0
+        // Prime the queue with planes z0-R .. z0+R-1.
 #pragma unroll
-                for (int p = 0; p <= 2 * R; ++p)
-                    pl[p] = ring + ((qlo + p) % S::NS) * (S::SLOT_BYTES / 4);
-                const float *c_row = pl[R] + (ty + R) * S::PW + 4 * tx;  // starts RA left of x
+        for (int p = 0; p < 2 * R; ++p) {
+            const uint32_t q = qb + p;
+            const int s = q & (NS - 1);
+            if (!mbar_wait_bounded(&full[s], (q / NS) & 1)) return;
+            const float *sl = ring + s * S::SLOT_FLOATS + own;
+#pragma unroll
+            for (int r = 0; r < RY; ++r) qz[r][p] = lds4(sl + r * S::PW);
+            if (p < R || p >= np - R) release(s);
+        }
+        for (int z = z0; z < z1; ++z) {
+            // Newest plane z+R: its own cells enter the queue.
+            {
+                const int pn = z - z0 + 2 * R;
+                const uint32_t q = qb + pn;
+                const int s = q & (NS - 1);
+                if (!mbar_wait_bounded(&full[s], (q / NS) & 1)) return;
+                const float *sl = ring + s * S::SLOT_FLOATS + own;
+#pragma unroll
+                for (int r = 0; r < RY; ++r) qz[r][2 * R] = lds4(sl + r * S::PW);
+                if (pn >= np - R) release(s);
+            }
+            // Centre plane z: x/y neighbours from its slot.
+            const int sc = (qb + (z - z0) + R) & (NS - 1);
+            const float *cb = ring + sc * S::SLOT_FLOATS + own;
+            float4 col[RY + 2 * R];  // the thread's 4 columns, rows -R .. RY-1+R
+#pragma unroll
+            for (int k = 0; k < RY + 2 * R; ++k) col[k] = lds4(cb + (k - R) * S::PW);
+            float acc[RY][4];
+#pragma unroll
+            for (int r = 0; r < RY; ++r) {
                 float w[4 + 2 * S::RA];
 #pragma unroll
-                for (int q = 0; q < (4 + 2 * S::RA) / 4; ++q) {
-                    const float4 v = *reinterpret_cast<const float4 *>(c_row + 4 * q);
-                    w[4 * q] = v.x; w[4 * q + 1] = v.y; w[4 * q + 2] = v.z; w[4 * q + 3] = v.w;
+                for (int h = 0; h < S::RA / 4; ++h) {
+                    const float4 a = lds4(cb + r * S::PW - S::RA + 4 * h);
+                    const float4 b = lds4(cb + r * S::PW + 4 + 4 * h);
+                    w[4 * h] = a.x; w[4 * h + 1] = a.y; w[4 * h + 2] = a.z; w[4 * h + 3] = a.w;
+                    w[S::RA + 4 + 4 * h] = b.x; w[S::RA + 5 + 4 * h] = b.y;
+                    w[S::RA + 6 + 4 * h] = b.z; w[S::RA + 7 + 4 * h] = b.w;
                 }
-                float acc[4] = {0.f, 0.f, 0.f, 0.f};
+                const float4 c = col[r + R];
+                w[S::RA] = c.x; w[S::RA + 1] = c.y; w[S::RA + 2] = c.z; w[S::RA + 3] = c.w;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[r][e] = 0.0f;
+                // axis i
 #pragma unroll
                 for (int o = -R; o <= R; ++o) {
                     if (o == 0) continue;
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) acc[e] += w[S::RA + e + o];
+                    for (int e = 0; e < 4; ++e) acc[r][e] += w[S::RA + e + o];
                 }
+                // axis j
 #pragma unroll
                 for (int o = -R; o <= R; ++o) {
                     if (o == 0) continue;
-                    const float4 v =
-                        *reinterpret_cast<const float4 *>(c_row + o * S::PW + S::RA);
-                    acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
+                    const float4 v = col[r + R + o];
+                    acc[r][0] += v.x; acc[r][1] += v.y; acc[r][2] += v.z; acc[r][3] += v.w;
                 }
+                // axis k
 #pragma unroll
                 for (int o = -R; o <= R; ++o) {
                     if (o == 0) continue;
-                    const float4 v = *reinterpret_cast<const float4 *>(
-                        pl[R + o] + (ty + R) * S::PW + 4 * tx + S::RA);
-                    acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
-                }
-                float out[4];
-#pragma unroll
-                for (int e = 0; e < 4; ++e)
-                    out[e] = star_finish<3, R>(acc[e], w[S::RA + e], g.legacy);
-                float *drow = dst + (long long)z * g.sz + (long long)y * g.sy;
-                if (x >= R && x + 3 < g.nx - R) {
-                    *reinterpret_cast<float4 *>(drow + x) =
-                        make_float4(out[0], out[1], out[2], out[3]);
-                } else {
-#pragma unroll
-                    for (int e = 0; e < 4; ++e)
-                        if (in_range(x + e, g.nx, R)) drow[x + e] = out[e];
+                    const float4 v = qz[r][R + o];
+                    acc[r][0] += v.x; acc[r][1] += v.y; acc[r][2] += v.z; acc[r][3] += v.w;
                 }
             }
-            // Every thread has finished reading plane z-R: its slot may be refilled.
-            if (!__syncthreads_and(ok)) return;
-            if (tid == 0) {
-                const int p = (z - z0) + S::NS;  // next plane of this item
-                if (p < np) {
-                    const uint32_t q = qbase + p;
-                    const int s = q % S::NS;
-                    mbar_arrive_expect_tx(&full[s], S::PLANE_BYTES);
-                    tma_load_3d(ring + s * (S::SLOT_BYTES / 4), &src_map, &full[s],
-                                x0 - S::RA, y0 - R, z0 - R + p);
+            // The centre slot is no longer read by this warp.
+            release(sc);
+            // Epilogue: correctly rounded division by 6R (warp-uniform fast path).
+            bool fast = true;
+#pragma unroll
+            for (int r = 0; r < RY; ++r)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) fast = fast && div_fast_ok<C>(acc[r][e]);
+            if (__all_sync(0xffffffffu, fast)) {
+#pragma unroll
+                for (int r = 0; r < RY; ++r)
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) acc[r][e] = div_fast<C>(acc[r][e]);
+            } else {
+#pragma unroll
+                for (int r = 0; r < RY; ++r)
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) acc[r][e] = acc[r][e] / (float)C;
+            }
+            if (g.legacy) {
+#pragma unroll
+                for (int r = 0; r < RY; ++r) {
+                    const float4 c = col[r + R];
+                    acc[r][0] -= c.x; acc[r][1] -= c.y; acc[r][2] -= c.z; acc[r][3] -= c.w;
                 }
             }
+            if (x < g.nx) {
+                float *dz = dst + (long long)z * g.sz;
+                const bool xin = x >= R && x + 3 < g.nx - R;
+#pragma unroll
+                for (int r = 0; r < RY; ++r) {
+                    const int y = ybase + r;
+                    if (!in_range(y, g.ny, R)) continue;
+                    float *drow = dz + (long long)y * g.sy;
+                    if (xin) {
+                        *reinterpret_cast<float4 *>(drow + x) =
+                            make_float4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 4; ++e)
+                            if (in_range(x + e, g.nx, R)) drow[x + e] = acc[r][e];
+                    }
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < RY; ++r)
+#pragma unroll
+                for (int k = 0; k < 2 * R; ++k) qz[r][k] = qz[r][k + 1];
         }
-        // Consume the completions of planes loaded but not waited on (the last
-        // 2R planes are waited inside the loop; nothing else is outstanding).
-        qbase += np;
+        qb += np;
     }
 }
 
@@ -158,21 +237,20 @@ struct StreamKernel {
     int tx, ty, threads, smem;
 };
 
-template <int R, int TX, int TY>
+template <int R, int TX, int TY, int RY, int NS>
 StreamKernel sk() {
-    using S = StreamShape<R, TX, TY>;
-    return {reinterpret_cast<const void *>(k_stream3d<R, TX, TY>), TX, TY, S::THREADS,
+    using S = StreamShape<R, TX, TY, RY, NS>;
+    return {reinterpret_cast<const void *>(k_stream3d<R, TX, TY, RY, NS>), TX, TY, S::THREADS,
             S::SMEM_BYTES};
 }
 
-StreamKernel pick(int r, int tile_x, int tile_y) {
-    const bool wide = tile_x >= 128;
-    const bool tall = tile_y >= 16;
+// shape: 0 = default (128 x 16), 1 = tall (64 x 32)
+StreamKernel pick(int r, int shape) {
     switch (r) {
-        case 1: return wide ? (tall ? sk<1, 128, 16>() : sk<1, 128, 8>()) : (tall ? sk<1, 64, 16>() : sk<1, 64, 8>());
-        case 2: return wide ? (tall ? sk<2, 128, 16>() : sk<2, 128, 8>()) : (tall ? sk<2, 64, 16>() : sk<2, 64, 8>());
-        case 3: return wide ? sk<3, 128, 8>() : sk<3, 64, 8>();
-        case 4: return wide ? (tall ? sk<4, 128, 16>() : sk<4, 128, 8>()) : (tall ? sk<4, 64, 16>() : sk<4, 64, 8>());
+        case 1: return shape == 1 ? sk<1, 64, 32, 4, 8>() : sk<1, 128, 16, 4, 8>();
+        case 2: return shape == 1 ? sk<2, 64, 32, 2, 8>() : sk<2, 128, 16, 2, 8>();
+        case 3: return shape == 1 ? sk<3, 64, 32, 2, 8>() : sk<3, 128, 16, 2, 8>();
+        case 4: return shape == 1 ? sk<4, 64, 32, 2, 8>() : sk<4, 128, 16, 2, 8>();
         default: return {nullptr, 0, 0, 0, 0};
     }
 }
@@ -186,7 +264,8 @@ bool stream3d_supported(const Geom &g) {
 int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int tile_y,
                  cudaStream_t s, float **res) {
     const int R = g.radius;
-    StreamKernel k = pick(R, tile_x ? tile_x : 128, tile_y ? tile_y : 16);
+    const int shape = (tile_x && tile_x < 128) || tile_y > 16 ? 1 : 0;
+    StreamKernel k = pick(R, shape);
     if (!k.fn) return fail(STENCIL_EUNSUPPORTED, "stream kernel has no radius-%d instance", R);
     if (g.nx % 4) return fail(STENCIL_EUNSUPPORTED, "stream kernel needs nx %% 4 == 0");
     ST_CUDA(cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, k.smem));
@@ -197,7 +276,7 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     const int tiles_x = (g.nx + k.tx - 1) / k.tx, tiles_y = (g.ny + k.ty - 1) / k.ty;
     const int tiles = tiles_x * tiles_y;
     const int zin = g.nz - 2 * R;
-    // About four waves of items so the tail is short, chunks of >= 8 planes.
+    // About four items per resident CTA so the tail is short; chunks >= 8 planes.
     int nchunks = std::max(1, (4 * resident + tiles - 1) / tiles);
     int zchunk = std::max(8, (zin + nchunks - 1) / nchunks);
     zchunk = std::min(zchunk, zin);
@@ -213,11 +292,11 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     if (rc) return rc;
     float *cur = a, *nxt = b;
     int ci = 0;
-    dim3 block(k.tx / 4, k.ty);
+    Geom gg = g;
+    int tx_ = tiles_x, ty_ = tiles_y, it_ = items;
     for (int it = 0; it < iters; ++it) {
-        void *args[] = {&maps[ci], &nxt, const_cast<Geom *>(&g), const_cast<int *>(&tiles_x),
-                        const_cast<int *>(&tiles_y), &zchunk, const_cast<int *>(&items)};
-        ST_CUDA(cudaLaunchKernel(k.fn, dim3(grid), block, args, k.smem, s));
+        void *args[] = {&maps[ci], &nxt, &gg, &tx_, &ty_, &zchunk, &it_};
+        ST_CUDA(cudaLaunchKernel(k.fn, dim3(grid), dim3(k.threads), args, k.smem, s));
         std::swap(cur, nxt);
         ci ^= 1;
     }

@@ -67,6 +67,9 @@ def load() -> ctypes.CDLL:
         "stencil_copy_border": (i, [P, vp, vp, vp]),
         "stencil_residual": (i, [P, vp, ctypes.POINTER(ctypes.c_double), vp]),
         "stencil_residual_noalloc": (i, [P, vp, ctypes.POINTER(ctypes.c_double), vp]),
+        "stencil_selftest_div": (i, [i, ctypes.POINTER(ctypes.c_ulonglong),
+                                     ctypes.POINTER(ctypes.c_uint)]),
+        "stencil_selftest_wait": (i, [i, ctypes.POINTER(i), ctypes.POINTER(i)]),
         "stencil_strerror": (ctypes.c_char_p, [i]),
         "stencil_last_error": (ctypes.c_char_p, []),
         "stencil_device_status": (i, [ctypes.POINTER(i)]),
