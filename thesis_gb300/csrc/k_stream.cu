@@ -13,7 +13,8 @@
 //   * consumer warps compute.  A consumer thread owns 4 consecutive cells of RY
 //     rows.  The z-neighbours of its cells live in a register queue of 2R+1
 //     planes (each plane's own cells are read from shared memory once, when
-//     the plane arrives); x- and y-neighbours come from the centre plane's
+//     the plane arrives; the z loop is unrolled 2R+1 times so the queue
+//     rotates without register moves); x- and y-neighbours come from the centre plane's
 //     slot with 16-byte shared loads.  So a slot is needed only while its
 //     plane is the newest or the centre: the ring holds R+1 planes plus the
 //     planes in flight.
@@ -52,7 +53,7 @@ struct StreamShape {
 __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 
 template <int R, int TX, int TY, int RY, int NS>
-__global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, 1)
+__global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <= 1 ? 2 : 1))
     k_stream3d(const __grid_constant__ CUtensorMap src_map, float *__restrict__ dst, Geom g,
                int tiles_x, int tiles_y, int zchunk, int items) {
     using S = StreamShape<R, TX, TY, RY, NS>;
@@ -101,8 +102,9 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, 1)
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);
     };
-    float4 qz[RY][2 * R + 1];  // z register queue: planes z-R .. z+R of this thread's cells
-    uint32_t qb = 0;           // sequence number of plane 0 of the current item
+    constexpr int QN = 2 * R + 1;
+    float4 qz[RY][QN];  // z register queue, rotated by unrolling: plane z+k-R sits at index (z-z0+k) % QN
+    uint32_t qb = 0;    // sequence number of plane 0 of the current item
     for (int item = blockIdx.x; item < items; item += gridDim.x) {
         const int t = item % ntiles, ch = item / ntiles;
         const int x0 = (t % tiles_x) * TX, y0 = (t / tiles_x) * TY;
@@ -110,7 +112,14 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, 1)
         const int np = (z1 - z0) + 2 * R;
         const int x = x0 + 4 * cx, ybase = y0 + cy * RY;
         const int own = (cy * RY + R) * S::PW + 4 * cx + S::RA;  // slot offset of row 0, cell 0
-        // Prime the queue with planes z0-R .. z0+R-1.
+        // Which of this thread's rows are stored, and whether its 4 cells are
+        // all inside the update region along x (16-byte store) or not.
+        unsigned live = 0;
+#pragma unroll
+        for (int r = 0; r < RY; ++r)
+            if (x < g.nx && in_range(ybase + r, g.ny, R)) live |= 1u << r;
+        const bool xin = x >= R && x + 3 < g.nx - R;
+        // Prime the queue with planes z0-R .. z0+R-1 (queue indices 0 .. 2R-1).
 #pragma unroll
         for (int p = 0; p < 2 * R; ++p) {
             const uint32_t q = qb + p;
@@ -121,110 +130,113 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, 1)
             for (int r = 0; r < RY; ++r) qz[r][p] = lds4(sl + r * S::PW);
             if (p < R || p >= np - R) release(s);
         }
-        for (int z = z0; z < z1; ++z) {
-            // Newest plane z+R: its own cells enter the queue.
-            {
-                const int pn = z - z0 + 2 * R;
-                const uint32_t q = qb + pn;
-                const int s = q & (NS - 1);
-                if (!mbar_wait_bounded(&full[s], (q / NS) & 1)) return;
-                const float *sl = ring + s * S::SLOT_FLOATS + own;
+        for (int zb = z0; zb < z1; zb += QN) {
 #pragma unroll
-                for (int r = 0; r < RY; ++r) qz[r][2 * R] = lds4(sl + r * S::PW);
-                if (pn >= np - R) release(s);
-            }
-            // Centre plane z: x/y neighbours from its slot.
-            const int sc = (qb + (z - z0) + R) & (NS - 1);
-            const float *cb = ring + sc * S::SLOT_FLOATS + own;
-            float4 col[RY + 2 * R];  // the thread's 4 columns, rows -R .. RY-1+R
+            for (int ph = 0; ph < QN; ++ph) {
+                const int z = zb + ph;
+                if (z >= z1) break;
+                // Newest plane z+R enters the queue at index (ph + 2R) % QN.
+                {
+                    const int pn = z - z0 + 2 * R;
+                    const uint32_t q = qb + pn;
+                    const int s = q & (NS - 1);
+                    if (!mbar_wait_bounded(&full[s], (q / NS) & 1)) return;
+                    const float *sl = ring + s * S::SLOT_FLOATS + own;
 #pragma unroll
-            for (int k = 0; k < RY + 2 * R; ++k) col[k] = lds4(cb + (k - R) * S::PW);
-            float acc[RY][4];
-#pragma unroll
-            for (int r = 0; r < RY; ++r) {
-                float w[4 + 2 * S::RA];
-#pragma unroll
-                for (int h = 0; h < S::RA / 4; ++h) {
-                    const float4 a = lds4(cb + r * S::PW - S::RA + 4 * h);
-                    const float4 b = lds4(cb + r * S::PW + 4 + 4 * h);
-                    w[4 * h] = a.x; w[4 * h + 1] = a.y; w[4 * h + 2] = a.z; w[4 * h + 3] = a.w;
-                    w[S::RA + 4 + 4 * h] = b.x; w[S::RA + 5 + 4 * h] = b.y;
-                    w[S::RA + 6 + 4 * h] = b.z; w[S::RA + 7 + 4 * h] = b.w;
+                    for (int r = 0; r < RY; ++r) qz[r][(ph + 2 * R) % QN] = lds4(sl + r * S::PW);
+                    if (pn >= np - R) release(s);
                 }
-                const float4 c = col[r + R];
-                w[S::RA] = c.x; w[S::RA + 1] = c.y; w[S::RA + 2] = c.z; w[S::RA + 3] = c.w;
+                // Centre plane z: x/y neighbours from its slot.
+                const int sc = (qb + (z - z0) + R) & (NS - 1);
+                const float *cb = ring + sc * S::SLOT_FLOATS + own;
+                float4 col[RY + 2 * R];  // the thread's 4 columns, rows -R .. RY-1+R
 #pragma unroll
-                for (int e = 0; e < 4; ++e) acc[r][e] = 0.0f;
-                // axis i
-#pragma unroll
-                for (int o = -R; o <= R; ++o) {
-                    if (o == 0) continue;
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) acc[r][e] += w[S::RA + e + o];
-                }
-                // axis j
-#pragma unroll
-                for (int o = -R; o <= R; ++o) {
-                    if (o == 0) continue;
-                    const float4 v = col[r + R + o];
-                    acc[r][0] += v.x; acc[r][1] += v.y; acc[r][2] += v.z; acc[r][3] += v.w;
-                }
-                // axis k
-#pragma unroll
-                for (int o = -R; o <= R; ++o) {
-                    if (o == 0) continue;
-                    const float4 v = qz[r][R + o];
-                    acc[r][0] += v.x; acc[r][1] += v.y; acc[r][2] += v.z; acc[r][3] += v.w;
-                }
-            }
-            // The centre slot is no longer read by this warp.
-            release(sc);
-            // Epilogue: correctly rounded division by 6R (warp-uniform fast path).
-            bool fast = true;
-#pragma unroll
-            for (int r = 0; r < RY; ++r)
-#pragma unroll
-                for (int e = 0; e < 4; ++e) fast = fast && div_fast_ok<C>(acc[r][e]);
-            if (__all_sync(0xffffffffu, fast)) {
-#pragma unroll
-                for (int r = 0; r < RY; ++r)
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) acc[r][e] = div_fast<C>(acc[r][e]);
-            } else {
-#pragma unroll
-                for (int r = 0; r < RY; ++r)
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) acc[r][e] = acc[r][e] / (float)C;
-            }
-            if (g.legacy) {
+                for (int k = 0; k < RY + 2 * R; ++k) col[k] = lds4(cb + (k - R) * S::PW);
+                float acc[RY][4];
 #pragma unroll
                 for (int r = 0; r < RY; ++r) {
+                    float w[4 + 2 * S::RA];
+#pragma unroll
+                    for (int h = 0; h < S::RA / 4; ++h) {
+                        const float4 a = lds4(cb + r * S::PW - S::RA + 4 * h);
+                        const float4 b = lds4(cb + r * S::PW + 4 + 4 * h);
+                        w[4 * h] = a.x; w[4 * h + 1] = a.y; w[4 * h + 2] = a.z; w[4 * h + 3] = a.w;
+                        w[S::RA + 4 + 4 * h] = b.x; w[S::RA + 5 + 4 * h] = b.y;
+                        w[S::RA + 6 + 4 * h] = b.z; w[S::RA + 7 + 4 * h] = b.w;
+                    }
                     const float4 c = col[r + R];
-                    acc[r][0] -= c.x; acc[r][1] -= c.y; acc[r][2] -= c.z; acc[r][3] -= c.w;
+                    w[S::RA] = c.x; w[S::RA + 1] = c.y; w[S::RA + 2] = c.z; w[S::RA + 3] = c.w;
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) acc[r][e] = 0.0f;
+                    // axis i
+#pragma unroll
+                    for (int o = -R; o <= R; ++o) {
+                        if (o == 0) continue;
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) acc[r][e] += w[S::RA + e + o];
+                    }
+                    // axis j
+#pragma unroll
+                    for (int o = -R; o <= R; ++o) {
+                        if (o == 0) continue;
+                        const float4 v = col[r + R + o];
+                        acc[r][0] += v.x; acc[r][1] += v.y; acc[r][2] += v.z; acc[r][3] += v.w;
+                    }
+                    // axis k: plane z+o is at queue index (ph + R + o) % QN
+#pragma unroll
+                    for (int o = -R; o <= R; ++o) {
+                        if (o == 0) continue;
+                        const float4 v = qz[r][(ph + R + o + QN) % QN];
+                        acc[r][0] += v.x; acc[r][1] += v.y; acc[r][2] += v.z; acc[r][3] += v.w;
+                    }
                 }
-            }
-            if (x < g.nx) {
-                float *dz = dst + (long long)z * g.sz;
-                const bool xin = x >= R && x + 3 < g.nx - R;
+                // The centre slot is no longer read by this warp.
+                release(sc);
+                // Epilogue: correctly rounded division by 6R.  The fast path
+                // applies when every stored sum lies in [2^-100, 2^120] (NaN
+                // sums pass through it as NaN); otherwise the warp divides.
+                float lo = 0x1p-100f, hi = 0x1p+120f;
+#pragma unroll
+                for (int r = 0; r < RY; ++r)
+                    if (live & (1u << r))
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            lo = fminf(lo, fabsf(acc[r][e]));
+                            hi = fmaxf(hi, fabsf(acc[r][e]));
+                        }
+                if (__all_sync(0xffffffffu, lo >= 0x1p-100f && hi <= 0x1p+120f)) {
+#pragma unroll
+                    for (int r = 0; r < RY; ++r)
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) acc[r][e] = div_fast<C>(acc[r][e]);
+                } else {
+#pragma unroll
+                    for (int r = 0; r < RY; ++r)
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) acc[r][e] = acc[r][e] / (float)C;
+                }
+                if (g.legacy) {
+#pragma unroll
+                    for (int r = 0; r < RY; ++r) {
+                        const float4 c = col[r + R];
+                        acc[r][0] -= c.x; acc[r][1] -= c.y; acc[r][2] -= c.z; acc[r][3] -= c.w;
+                    }
+                }
+                float *dz = dst + (long long)z * g.sz + (long long)ybase * g.sy + x;
 #pragma unroll
                 for (int r = 0; r < RY; ++r) {
-                    const int y = ybase + r;
-                    if (!in_range(y, g.ny, R)) continue;
-                    float *drow = dz + (long long)y * g.sy;
+                    if (!(live & (1u << r))) continue;
+                    float *d = dz + (long long)r * g.sy;
                     if (xin) {
-                        *reinterpret_cast<float4 *>(drow + x) =
+                        *reinterpret_cast<float4 *>(d) =
                             make_float4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
                     } else {
 #pragma unroll
                         for (int e = 0; e < 4; ++e)
-                            if (in_range(x + e, g.nx, R)) drow[x + e] = acc[r][e];
+                            if (in_range(x + e, g.nx, R)) d[e] = acc[r][e];
                     }
                 }
             }
-#pragma unroll
-            for (int r = 0; r < RY; ++r)
-#pragma unroll
-                for (int k = 0; k < 2 * R; ++k) qz[r][k] = qz[r][k + 1];
         }
         qb += np;
     }
@@ -247,7 +259,7 @@ StreamKernel sk() {
 // shape: 0 = default (128 x 16), 1 = tall (64 x 32)
 StreamKernel pick(int r, int shape) {
     switch (r) {
-        case 1: return shape == 1 ? sk<1, 64, 32, 4, 8>() : sk<1, 128, 16, 4, 8>();
+        case 1: return shape == 1 ? sk<1, 64, 32, 2, 8>() : sk<1, 128, 16, 2, 8>();
         case 2: return shape == 1 ? sk<2, 64, 32, 2, 8>() : sk<2, 128, 16, 2, 8>();
         case 3: return shape == 1 ? sk<3, 64, 32, 2, 8>() : sk<3, 128, 16, 2, 8>();
         case 4: return shape == 1 ? sk<4, 64, 32, 2, 8>() : sk<4, 128, 16, 2, 8>();
