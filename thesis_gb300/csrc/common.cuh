@@ -238,6 +238,13 @@ __device__ __forceinline__ float ld_cluster_f32(uint32_t addr) {
     return v;
 }
 
+// 16-byte global store that the compiler cannot split into scalar stores.
+__device__ __forceinline__ void stg4(float *p, float a, float b, float c, float d) {
+    asm volatile("st.global.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c),
+                 "f"(d)
+                 : "memory");
+}
+
 __device__ __forceinline__ float f4get(const float4 &v, int c) {
     return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
 }

@@ -130,25 +130,17 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
             for (int r = 0; r < RY; ++r) qz[r][p] = lds4(sl + r * S::PW);
             if (p < R || p >= np - R) release(s);
         }
+        float *drow = dst + (long long)z0 * g.sz + (long long)ybase * g.sy + x;
+        const float *ring_own = ring + own;
         for (int zb = z0; zb < z1; zb += QN) {
 #pragma unroll
             for (int ph = 0; ph < QN; ++ph) {
                 const int z = zb + ph;
                 if (z >= z1) break;
-                // Newest plane z+R enters the queue at index (ph + 2R) % QN.
-                {
-                    const int pn = z - z0 + 2 * R;
-                    const uint32_t q = qb + pn;
-                    const int s = q & (NS - 1);
-                    if (!mbar_wait_bounded(&full[s], (q / NS) & 1)) return;
-                    const float *sl = ring + s * S::SLOT_FLOATS + own;
-#pragma unroll
-                    for (int r = 0; r < RY; ++r) qz[r][(ph + 2 * R) % QN] = lds4(sl + r * S::PW);
-                    if (pn >= np - R) release(s);
-                }
-                // Centre plane z: x/y neighbours from its slot.
-                const int sc = (qb + (z - z0) + R) & (NS - 1);
-                const float *cb = ring + sc * S::SLOT_FLOATS + own;
+                const int step = z - z0;
+                // Centre plane z (already waited on as the newest, R steps ago).
+                const int sc = (qb + step + R) & (NS - 1);
+                const float *cb = ring_own + sc * S::SLOT_FLOATS;
                 float4 col[RY + 2 * R];  // the thread's 4 columns, rows -R .. RY-1+R
 #pragma unroll
                 for (int k = 0; k < RY + 2 * R; ++k) col[k] = lds4(cb + (k - R) * S::PW);
@@ -182,16 +174,35 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
                         const float4 v = col[r + R + o];
                         acc[r][0] += v.x; acc[r][1] += v.y; acc[r][2] += v.z; acc[r][3] += v.w;
                     }
-                    // axis k: plane z+o is at queue index (ph + R + o) % QN
+                    // axis k, previous planes z-R .. z-1 (queue indices (ph + R + o) % QN)
 #pragma unroll
-                    for (int o = -R; o <= R; ++o) {
-                        if (o == 0) continue;
+                    for (int o = -R; o <= -1; ++o) {
                         const float4 v = qz[r][(ph + R + o + QN) % QN];
                         acc[r][0] += v.x; acc[r][1] += v.y; acc[r][2] += v.z; acc[r][3] += v.w;
                     }
                 }
                 // The centre slot is no longer read by this warp.
                 release(sc);
+                // Newest plane z+R enters the queue at index (ph + 2R) % QN;
+                // waiting for it overlaps the work above.
+                {
+                    const int pn = step + 2 * R;
+                    const uint32_t q = qb + pn;
+                    const int s = q & (NS - 1);
+                    if (!mbar_wait_bounded(&full[s], (q / NS) & 1)) return;
+                    const float *sl = ring_own + s * S::SLOT_FLOATS;
+#pragma unroll
+                    for (int r = 0; r < RY; ++r) qz[r][(ph + 2 * R) % QN] = lds4(sl + r * S::PW);
+                    if (pn >= np - R) release(s);
+                }
+                // axis k, next planes z+1 .. z+R
+#pragma unroll
+                for (int r = 0; r < RY; ++r)
+#pragma unroll
+                    for (int o = 1; o <= R; ++o) {
+                        const float4 v = qz[r][(ph + R + o) % QN];
+                        acc[r][0] += v.x; acc[r][1] += v.y; acc[r][2] += v.z; acc[r][3] += v.w;
+                    }
                 // Epilogue: correctly rounded division by 6R.  The fast path
                 // applies when every stored sum lies in [2^-100, 2^120] (NaN
                 // sums pass through it as NaN); otherwise the warp divides.
@@ -222,20 +233,20 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
                         acc[r][0] -= c.x; acc[r][1] -= c.y; acc[r][2] -= c.z; acc[r][3] -= c.w;
                     }
                 }
-                float *dz = dst + (long long)z * g.sz + (long long)ybase * g.sy + x;
+                if (xin) {
 #pragma unroll
-                for (int r = 0; r < RY; ++r) {
-                    if (!(live & (1u << r))) continue;
-                    float *d = dz + (long long)r * g.sy;
-                    if (xin) {
-                        *reinterpret_cast<float4 *>(d) =
-                            make_float4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
-                    } else {
+                    for (int r = 0; r < RY; ++r)
+                        if (live & (1u << r))
+                            stg4(drow + r * g.sy, acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
+                } else {
 #pragma unroll
-                        for (int e = 0; e < 4; ++e)
-                            if (in_range(x + e, g.nx, R)) d[e] = acc[r][e];
-                    }
+                    for (int r = 0; r < RY; ++r)
+                        if (live & (1u << r))
+#pragma unroll
+                            for (int e = 0; e < 4; ++e)
+                                if (in_range(x + e, g.nx, R)) drow[r * g.sy + e] = acc[r][e];
                 }
+                drow += g.sz;
             }
         }
         qb += np;
