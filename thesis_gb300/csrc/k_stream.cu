@@ -22,12 +22,14 @@
 // used by an updated cell.  Each input cell is read from HBM once per sweep;
 // halos of neighbouring tiles and chunks are re-read from L2.
 //
-// Work items are (tile, z-chunk) pairs, chunk-major so that co-resident CTAs
-// work on neighbouring tiles of one z range.  CTAs loop over items; the
-// producer and the consumers walk the same item sequence, and a monotone plane
-// sequence number fixes each plane's slot and mbarrier phase.  No CTA-wide
+// Work: the (tile, z-plane) steps in tile-major order are split into equal
+// contiguous shares, one per resident CTA; a share covers one or a few
+// (tile, z-range) segments.  The producer and the consumers walk the same
+// segments, and a monotone plane sequence number fixes each plane's slot and
+// mbarrier phase.  No CTA-wide
 // barrier is used after set-up, and every mbarrier wait is bounded.
 #include <algorithm>
+#include <cmath>
 
 #include "host.hpp"
 
@@ -55,7 +57,7 @@ __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cas
 template <int R, int TX, int TY, int RY, int NS>
 __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <= 1 ? 2 : 1))
     k_stream3d(const __grid_constant__ CUtensorMap src_map, float *__restrict__ dst, Geom g,
-               int tiles_x, int tiles_y, int zchunk, int items) {
+               int tiles_x, long long total) {
     using S = StreamShape<R, TX, TY, RY, NS>;
     constexpr int C = 6 * R;  // 2*D*R with D = 3
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -73,16 +75,22 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
         fence_mbar_init();
     }
     __syncthreads();
-    const int ntiles = tiles_x * tiles_y;
+    // This CTA's share of the (tile, plane) steps: [lo, hi) in tile-major order.
+    const int zin = g.nz - 2 * R;
+    const long long lo = total * blockIdx.x / gridDim.x;
+    const long long hi = total * (blockIdx.x + 1) / gridDim.x;
 
     if (warp == S::CWARPS) {
         // ---------------- producer ----------------
         if (lane != 0) return;
         uint32_t q = 0;
-        for (int item = blockIdx.x; item < items; item += gridDim.x) {
-            const int t = item % ntiles, ch = item / ntiles;
+        for (long long i = lo; i < hi;) {
+            const int t = (int)(i / zin);
+            const int z0 = R + (int)(i - (long long)t * zin);
+            const long long rem_ = hi - (long long)t * zin;
+            const int z1 = R + (int)(rem_ < zin ? rem_ : (long long)zin);
+            i = (long long)t * zin + (z1 - R);
             const int x0 = (t % tiles_x) * TX, y0 = (t / tiles_x) * TY;
-            const int z0 = R + ch * zchunk, z1 = min(z0 + zchunk, g.nz - R);
             const int np = (z1 - z0) + 2 * R;
             for (int p = 0; p < np; ++p, ++q) {
                 const int s = q & (NS - 1);
@@ -104,11 +112,14 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
     };
     constexpr int QN = 2 * R + 1;
     float4 qz[RY][QN];  // z register queue, rotated by unrolling: plane z+k-R sits at index (z-z0+k) % QN
-    uint32_t qb = 0;    // sequence number of plane 0 of the current item
-    for (int item = blockIdx.x; item < items; item += gridDim.x) {
-        const int t = item % ntiles, ch = item / ntiles;
+    uint32_t qb = 0;    // sequence number of plane 0 of the current segment
+    for (long long i = lo; i < hi;) {
+        const int t = (int)(i / zin);
+        const int z0 = R + (int)(i - (long long)t * zin);
+        const long long rem_ = hi - (long long)t * zin;
+            const int z1 = R + (int)(rem_ < zin ? rem_ : (long long)zin);
+        i = (long long)t * zin + (z1 - R);
         const int x0 = (t % tiles_x) * TX, y0 = (t / tiles_x) * TY;
-        const int z0 = R + ch * zchunk, z1 = min(z0 + zchunk, g.nz - R);
         const int np = (z1 - z0) + 2 * R;
         const int x = x0 + 4 * cx, ybase = y0 + cy * RY;
         const int own = (cy * RY + R) * S::PW + 4 * cx + S::RA;  // slot offset of row 0, cell 0
@@ -299,14 +310,11 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     const int tiles_x = (g.nx + k.tx - 1) / k.tx, tiles_y = (g.ny + k.ty - 1) / k.ty;
     const int tiles = tiles_x * tiles_y;
     const int zin = g.nz - 2 * R;
-    // About four items per resident CTA so the tail is short; chunks >= 8 planes.
-    int nchunks = std::max(1, (4 * resident + tiles - 1) / tiles);
-    int zchunk = std::max(8, (zin + nchunks - 1) / nchunks);
-    zchunk = std::min(zchunk, zin);
-    nchunks = (zin + zchunk - 1) / zchunk;
-    const int items = tiles * nchunks;
-    const int grid = std::min(items, resident);
-
+    // Every resident CTA gets an equal contiguous share of the tile-major
+    // (tile, plane) steps: no partly filled last wave, and at most a few
+    // segments (each re-reads 2R halo planes) per CTA.
+    const long long total = (long long)tiles * zin;
+    const int grid = (int)std::min<long long>(resident, total);
     CUtensorMap maps[2];
     const long long dims[3] = {g.nx, g.ny, g.nz};
     const int box[3] = {k.tx + 2 * ((R + 3) & ~3), k.ty + 2 * R, 1};
@@ -316,9 +324,10 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     float *cur = a, *nxt = b;
     int ci = 0;
     Geom gg = g;
-    int tx_ = tiles_x, ty_ = tiles_y, it_ = items;
+    int tx_ = tiles_x;
+    long long tot_ = total;
     for (int it = 0; it < iters; ++it) {
-        void *args[] = {&maps[ci], &nxt, &gg, &tx_, &ty_, &zchunk, &it_};
+        void *args[] = {&maps[ci], &nxt, &gg, &tx_, &tot_};
         ST_CUDA(cudaLaunchKernel(k.fn, dim3(grid), dim3(k.threads), args, k.smem, s));
         std::swap(cur, nxt);
         ci ^= 1;
