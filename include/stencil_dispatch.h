@@ -121,6 +121,36 @@ STENCIL_API int stencil_init_uniform(float *d_u, size_t count, uint64_t seed, st
 STENCIL_API int stencil_copy_border(const stencil_params *p, const float *d_src, float *d_dst,
                         stencil_stream_t stream);
 
+/* ---- Batched persistent sweeps: many grids of uneven sizes and sweep counts
+ * in ONE launch over a device work queue (no counterpart in the reference,
+ * which runs one grid per process).  Each job is one grid with its own two
+ * buffers; after the launch its result is in d_u1 for an even sweep count and
+ * in d_u2 for an odd one, exactly as stencil_dispatch_ex would leave it.
+ * Jobs need nx % 4 == 0 and radius <= 4. */
+typedef struct stencil_batch_job {
+    float *d_u1, *d_u2;
+    int dims, nx, ny, nz;
+    int radius, iterations, mode;
+    int reserved; /* must be zero */
+} stencil_batch_job;
+
+/* Device workspace bytes for njobs jobs (a job table and the queue counter). */
+STENCIL_API int stencil_batch_workspace_bytes(int njobs, size_t *bytes);
+/* Validates the jobs, orders them largest first and writes the job table into
+ * d_workspace (256-byte aligned, caller-owned).  cluster_size: CTAs per
+ * cluster (8 or 16; 0 = the largest the device schedules).  Synchronises
+ * `stream`. */
+STENCIL_API int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, int cluster_size,
+                                      void *d_workspace, size_t workspace_bytes,
+                                      stencil_stream_t stream);
+/* One persistent launch over the prepared jobs: resets the queue counter and
+ * launches every cluster the device can hold.  Asynchronous; allocates
+ * nothing; can be captured into a CUDA graph (the queue reset is a memset
+ * node, so every replay runs the whole batch again). */
+STENCIL_API int stencil_batch_launch(const void *d_workspace, stencil_stream_t stream);
+/* Drops the host-side record of a prepared workspace (call before freeing it). */
+STENCIL_API int stencil_batch_forget(const void *d_workspace);
+
 /* Relative residual ||b - A u||_2 / ||b||_2 of the steady state that JACOBI
  * iterates to, (A u)(x) = u(x) - mean of the 2*D*R axis neighbours over the
  * update region, b = the border contributions; squares summed in FP64 on the

@@ -162,9 +162,12 @@ static int ws_scratch(int dev, size_t bytes, void **out) {
     return STENCIL_OK;
 }
 
-// Variant choice when the caller leaves it to the library.
+// Variant choice when the caller leaves it to the library: grids that fit a
+// cluster's shared memory run all sweeps in one cluster launch (launch- and
+// sync-bound otherwise); large 3-D grids stream; the rest use the base kernel.
 static int choose_variant(const stencil_params &p) {
     const Geom g = make_geom(p);
+    if (p.iterations >= 8 && cluster_resident(g, p.dims)) return STENCIL_VARIANT_CLUSTER;
     if (p.dims == 3 && stream3d_supported(g)) return STENCIL_VARIANT_SMEM_REGISTER;
     return STENCIL_VARIANT_BASE;
 }
@@ -228,7 +231,19 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
     if ((variant == STENCIL_VARIANT_SMEM || variant == STENCIL_VARIANT_SMEM_PADDED) &&
         !tile_supported(g, p->dims))
         variant = STENCIL_VARIANT_BASE;
-    if (variant == STENCIL_VARIANT_COOP || variant == STENCIL_VARIANT_CLUSTER)
+    if (variant == STENCIL_VARIANT_COOP && cluster_resident(g, p->dims))
+        variant = STENCIL_VARIANT_CLUSTER;
+    if (variant == STENCIL_VARIANT_CLUSTER) {
+        if (g.nx % 4 == 0 && g.radius <= 4) {
+            float *res = nullptr;
+            rc = run_cluster(g, p->dims, cur, nxt, p->iterations, s, &res);
+            if (rc) return rc;
+            if (d_result) *d_result = res;
+            return STENCIL_OK;
+        }
+        variant = STENCIL_VARIANT_COOP;
+    }
+    if (variant == STENCIL_VARIANT_COOP)
         variant = p->dims == 3 && stream3d_supported(g) ? STENCIL_VARIANT_SMEM_REGISTER
                                                         : STENCIL_VARIANT_BASE;
     if (variant == STENCIL_VARIANT_SMEM_REGISTER) {

@@ -43,8 +43,11 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
                  cudaStream_t s, float **res);
 int run_tb3d(const Geom &g, float *a, float *b, int iters, int temporal, cudaStream_t s,
              float **res);
-int run_cluster2d(const Geom &g, float *a, float *b, int iters, cudaStream_t s, float **res);
-bool cluster2d_fits(const Geom &g);
+// All sweeps of one grid on one thread-block cluster (k_cluster.cu).
+int run_cluster(const Geom &g, int dims, float *a, float *b, int iters, cudaStream_t s,
+                float **res);
+// The grid fits the cluster's shared memory (resident mode).
+bool cluster_resident(const Geom &g, int dims);
 
 // Plain whole-grid helpers.
 int launch_copy_border(const Geom &g, int dims, const float *src, float *dst, cudaStream_t s);

@@ -1,0 +1,527 @@
+// k_cluster.cu -- the cluster engine: one thread-block cluster runs every sweep
+// of one grid in a single persistent launch ("coop" role,
+// src/stencil_kernel_coop.cu:5-49, whose launch the reference left commented
+// out at src/stencil_dispatch.cu:160-177), and a batch of grids of uneven
+// sizes and sweep counts runs as one launch over a device work queue.
+//
+// The slowest axis (rows in 2-D, planes in 3-D) is split into slabs, one per
+// CTA of the cluster.  Per sweep every CTA updates its slab, then the cluster
+// synchronises with the hardware cluster barrier (release/acquire at cluster
+// scope) -- the grid-wide sync of the reference's coop kernel, restricted to
+// the CTAs that share the grid.  Two storage modes:
+//   * resident: both ping-pong buffers of the slab plus R halo slices on each
+//     side live in shared memory; after a sweep each CTA pushes its first and
+//     last R slices into its neighbours' halos through distributed shared
+//     memory (st.shared::cluster), so HBM is touched only to load and store
+//     the grid once per launch;
+//   * global: the slabs are swept from global memory (L2-resident for the
+//     batch sizes) with the same per-cell code.
+// Cells outside the update region are never written, and both buffers are
+// loaded from the caller's two buffers, so LEGACY (second-buffer border) and
+// JACOBI semantics are exactly those of the ping-pong loop; at the end both
+// global buffers hold what the ping-pong loop leaves (last sweep in the result
+// buffer, the sweep before in the other).
+//
+// Work queue: CTA rank 0 of each cluster takes the next job index with an
+// atomic on a device counter and shares it through distributed shared memory.
+// Jobs are ordered by the host (largest first).  Every wait is a hardware
+// cluster barrier: no spin loops.
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "host.hpp"
+
+namespace st {
+
+struct ClusterJob {
+    float *a, *b;       // caller buffers (a = initial state)
+    int dims, nx, ny, nz;
+    int radius, iters, legacy, resident;
+};
+
+constexpr int kClusterThreads = 256;
+
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+
+// One sweep of the cells of slices [s_begin, s_end) (global slice indices).
+// src/dst address slice s at (s - base) * slice_len; the slice stride is
+// slice_len; within a slice the row pitch is nx.  Rows of the update region
+// only; float4 chunks (nx % 4 == 0 required).
+template <int D, int R>
+__device__ __forceinline__ void sweep_slab(const float *src, float *dst, long long base,
+                                           int s_begin, int s_end, const ClusterJob &j) {
+    constexpr int C = 2 * D * R;
+    const int nx = j.nx, ny = j.ny;
+    const long long slice_len = D == 3 ? (long long)nx * ny : nx;
+    const int chunks = nx >> 2;
+    const int rows = D == 3 ? ny - 2 * R : 1;  // update rows per slice
+    const int S = D == 3 ? j.nz : ny;
+    const int sb = max(s_begin, R), se = min(s_end, S - R);
+    if (sb >= se) return;
+    const long long units = (long long)(se - sb) * rows * chunks;
+    for (long long u = threadIdx.x; u < units; u += blockDim.x) {
+        const int c = (int)(u % chunks);
+        const long long rs = u / chunks;
+        const int row = D == 3 ? R + (int)(rs % rows) : 0;
+        const int s = sb + (int)(rs / rows);
+        const int x0 = c * 4;
+        if (x0 + 3 < R || x0 >= nx - R) continue;
+        const long long off = (long long)(s - base) * slice_len + (long long)row * nx + x0;
+        const float *p = src + off;
+        float w[4 + 2 * ((R + 3) & ~3)];
+        constexpr int RA = (R + 3) & ~3;
+#pragma unroll
+        for (int h = 0; h < (4 + 2 * RA) / 4; ++h) {
+            const int cc = c - RA / 4 + h;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (cc >= 0 && cc < chunks) v = ld4(p - RA + 4 * h);
+            w[4 * h] = v.x; w[4 * h + 1] = v.y; w[4 * h + 2] = v.z; w[4 * h + 3] = v.w;
+        }
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int o = -R; o <= R; ++o) {
+            if (!o) continue;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[e] += w[RA + e + o];
+        }
+        // axis j: the next row (3-D) or the next slice (2-D)
+        const long long sj = D == 3 ? nx : slice_len;
+#pragma unroll
+        for (int o = -R; o <= R; ++o) {
+            if (!o) continue;
+            const float4 v = ld4(p + o * sj);
+            acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
+        }
+        if (D == 3) {
+#pragma unroll
+            for (int o = -R; o <= R; ++o) {
+                if (!o) continue;
+                const float4 v = ld4(p + o * slice_len);
+                acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
+            }
+        }
+        float out[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            out[e] = div_coeff<C>(acc[e]);
+            if (j.legacy) out[e] -= w[RA + e];
+        }
+        float *q = dst + off;
+        if (x0 >= R && x0 + 3 < nx - R) {
+            *reinterpret_cast<float4 *>(q) = make_float4(out[0], out[1], out[2], out[3]);
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (x0 + e >= R && x0 + e < nx - R) q[e] = out[e];
+        }
+    }
+}
+
+// Copies slices [s_begin, s_end) between a global grid and a local slab.
+__device__ __forceinline__ void copy_slices(float *to, const float *from, long long count4) {
+    for (long long i = threadIdx.x; i < count4; i += blockDim.x)
+        reinterpret_cast<float4 *>(to)[i] = reinterpret_cast<const float4 *>(from)[i];
+}
+
+template <int D, int R>
+__device__ void run_job(const ClusterJob &j, float *smem, uint32_t rank, uint32_t csize) {
+    const int S = D == 3 ? j.nz : j.ny;
+    const long long slice_len = D == 3 ? (long long)j.nx * j.ny : j.nx;
+    const int H = (S + csize - 1) / csize;
+    const int s0 = min((int)rank * H, S), s1 = min(s0 + H, S);
+    if (j.resident) {
+        // Slab with halo: local slice k <-> global slice s0 - R + k.
+        const long long slab = (long long)(H + 2 * R) * slice_len;
+        float *buf[2] = {smem, smem + slab};
+        const int l0 = max(s0 - R, 0), l1 = min(s1 + R, S);
+        if (l0 < l1) {
+            const long long off = (long long)(l0 - (s0 - R)) * slice_len;
+            copy_slices(buf[0] + off, j.a + (long long)l0 * slice_len, (l1 - l0) * slice_len / 4);
+            copy_slices(buf[1] + off, j.b + (long long)l0 * slice_len, (l1 - l0) * slice_len / 4);
+        }
+        cluster_sync();
+        const uint32_t my0 = smem_u32(buf[0]);
+        int cur = 0;
+        for (int it = 0; it < j.iters; ++it) {
+            sweep_slab<D, R>(buf[cur], buf[cur ^ 1], s0 - R, s0, s1, j);
+            __syncthreads();
+            // Push the first / last R owned slices into the neighbours' halos.
+            const long long n4 = (long long)R * slice_len / 4;
+            const uint32_t dst_base = my0 + (uint32_t)((cur ^ 1) * slab * 4);
+            if (rank > 0 && s1 > s0) {
+                // my slices s0..s0+R-1 -> rank-1's local slices H+R .. H+2R-1
+                const float4 *from = reinterpret_cast<const float4 *>(buf[cur ^ 1] + (long long)R * slice_len);
+                const uint32_t to = mapa_shared(dst_base + (uint32_t)((long long)(H + R) * slice_len * 4), rank - 1);
+                for (long long i = threadIdx.x; i < n4; i += blockDim.x) st_cluster_v4(to + (uint32_t)(i * 16), from[i]);
+            }
+            if (rank + 1 < csize && s1 > s0 && s1 < S) {
+                // my slices s1-R..s1-1 -> rank+1's local slices 0..R-1
+                const float4 *from = reinterpret_cast<const float4 *>(buf[cur ^ 1] + (long long)(s1 - R - (s0 - R)) * slice_len);
+                const uint32_t to = mapa_shared(dst_base, rank + 1);
+                for (long long i = threadIdx.x; i < n4; i += blockDim.x) st_cluster_v4(to + (uint32_t)(i * 16), from[i]);
+            }
+            cluster_sync();
+            cur ^= 1;
+        }
+        // Both buffers back to the caller's buffers (owned slices only).
+        if (s1 > s0) {
+            const long long off = (long long)R * slice_len;
+            float *ga = (j.iters & 1) ? j.b : j.a;  // holds buf[cur]
+            float *gb = (j.iters & 1) ? j.a : j.b;
+            copy_slices(ga + (long long)s0 * slice_len, buf[cur] + off, (s1 - s0) * slice_len / 4);
+            copy_slices(gb + (long long)s0 * slice_len, buf[cur ^ 1] + off, (s1 - s0) * slice_len / 4);
+        }
+        cluster_sync();  // the slab is reused by the next job
+    } else {
+        const float *src = j.a;
+        float *dst = j.b;
+        for (int it = 0; it < j.iters; ++it) {
+            sweep_slab<D, R>(src, dst, 0, s0, s1, j);
+            cluster_sync();
+            const float *t = src;
+            src = dst;
+            dst = const_cast<float *>(t);
+        }
+    }
+}
+
+// queue == nullptr: the single job `one` (one cluster).  Otherwise clusters
+// take job indices from *queue until it passes njobs.
+__global__ void __launch_bounds__(kClusterThreads)
+    k_cluster(ClusterJob one, const ClusterJob *__restrict__ jobs, int njobs, unsigned *queue) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ int s_job;
+    __shared__ int s_jid;
+    float *smem = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
+                                            ~static_cast<uintptr_t>(127));
+    const uint32_t rank = cluster_ctarank(), csize = cluster_nctarank();
+    const uint32_t job_addr = mapa_shared(smem_u32(&s_job), 0);
+    for (int round = 0;; ++round) {
+        int jid;
+        if (queue) {
+            if (rank == 0 && threadIdx.x == 0) s_job = (int)atomicAdd(queue, 1u);
+            cluster_sync();
+            if (threadIdx.x == 0) {
+                int v;
+                asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(job_addr) : "memory");
+                s_jid = v;
+            }
+            __syncthreads();
+            jid = s_jid;
+            cluster_sync();  // rank 0 overwrites s_job only after everyone read it
+        } else {
+            jid = round;
+            njobs = 1;
+        }
+        if (jid >= njobs) break;
+        const ClusterJob j = queue ? jobs[jid] : one;
+        if (j.dims == 3) {
+            switch (j.radius) {
+                case 1: run_job<3, 1>(j, smem, rank, csize); break;
+                case 2: run_job<3, 2>(j, smem, rank, csize); break;
+                case 3: run_job<3, 3>(j, smem, rank, csize); break;
+                case 4: run_job<3, 4>(j, smem, rank, csize); break;
+            }
+        } else {
+            switch (j.radius) {
+                case 1: run_job<2, 1>(j, smem, rank, csize); break;
+                case 2: run_job<2, 2>(j, smem, rank, csize); break;
+                case 3: run_job<2, 3>(j, smem, rank, csize); break;
+                case 4: run_job<2, 4>(j, smem, rank, csize); break;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+constexpr int kClusterSmemMax = 200 * 1024;
+
+static long long slab_bytes(const ClusterJob &j, int csize) {
+    const int S = j.dims == 3 ? j.nz : j.ny;
+    const long long slice_len = j.dims == 3 ? (long long)j.nx * j.ny : j.nx;
+    const int H = (S + csize - 1) / csize;
+    return 2LL * (H + 2 * j.radius) * slice_len * 4;
+}
+
+bool cluster_job_ok(int dims, int nx, int ny, int nz, int radius) {
+    (void)ny; (void)nz; (void)dims;
+    return nx % 4 == 0 && radius >= 1 && radius <= 4;
+}
+
+// Resident when the slab fits and every CTA that owns slices owns at least R
+// (so each halo comes from one neighbour).
+static void plan_job(ClusterJob &j, int csize) {
+    const int S = j.dims == 3 ? j.nz : j.ny;
+    const int H = (S + csize - 1) / csize;
+    const int last = S - ((S + H - 1) / H - 1) * H;
+    j.resident = (slab_bytes(j, csize) + 128 <= kClusterSmemMax && H >= j.radius &&
+                  last >= j.radius) ? 1 : 0;
+}
+
+// Function attributes of k_cluster (once per device, outside any capture).
+static int ensure_cluster_attrs() {
+    static bool done[64] = {false};
+    const int d = current_device();
+    if (d >= 0 && d < 64 && done[d]) return STENCIL_OK;
+    ST_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void *>(k_cluster),
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    ST_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void *>(k_cluster),
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kClusterSmemMax + 128));
+    if (d >= 0 && d < 64) done[d] = true;
+    return STENCIL_OK;
+}
+
+int cluster_size_for_device() {
+    static int cached = 0;
+    if (cached) return cached;
+    int v = 0;
+    ensure_cluster_attrs();
+    for (int c : {16, 8}) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = c;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(c);
+        cfg.blockDim = dim3(kClusterThreads);
+        cfg.dynamicSmemBytes = kClusterSmemMax + 128;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        if (cudaOccupancyMaxActiveClusters(&v, reinterpret_cast<const void *>(k_cluster), &cfg) ==
+                cudaSuccess && v > 0) {
+            cached = c;
+            return c;
+        }
+        cudaGetLastError();
+    }
+    cached = 8;
+    return cached;
+}
+
+// Launches `clusters` clusters over the jobs (already in device memory).
+int launch_cluster_jobs(const ClusterJob *d_jobs, int njobs, unsigned *d_queue, int clusters,
+                        int csize, cudaStream_t s) {
+    ST_CUDA(cudaMemsetAsync(d_queue, 0, sizeof(unsigned), s));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = csize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(clusters * csize);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.dynamicSmemBytes = kClusterSmemMax + 128;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    ClusterJob none = {};
+    ST_CUDA(cudaLaunchKernelEx(&cfg, k_cluster, none, d_jobs, njobs, d_queue));
+    return STENCIL_OK;
+}
+
+int max_active_clusters(int csize) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = csize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(csize);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.dynamicSmemBytes = kClusterSmemMax + 128;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int v = 0;
+    if (cudaOccupancyMaxActiveClusters(&v, reinterpret_cast<const void *>(k_cluster), &cfg) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return std::max(1, v);
+}
+
+ClusterJob make_job(const Geom &g, int dims, float *a, float *b, int iters, int csize) {
+    ClusterJob j;
+    j.a = a;
+    j.b = b;
+    j.dims = dims;
+    j.nx = g.nx;
+    j.ny = g.ny;
+    j.nz = dims == 3 ? g.nz : 1;
+    j.radius = g.radius;
+    j.iters = iters;
+    j.legacy = g.legacy;
+    plan_job(j, csize);
+    return j;
+}
+
+size_t cluster_job_size() { return sizeof(ClusterJob); }
+
+// Single grid on one cluster, all sweeps in one launch (queue-less mode).
+int run_cluster(const Geom &g, int dims, float *a, float *b, int iters, cudaStream_t s,
+                float **res) {
+    if (g.nx % 4 || g.radius < 1 || g.radius > 4)
+        return fail(STENCIL_EUNSUPPORTED, "cluster engine needs nx %% 4 == 0 and R <= 4");
+    const int csize = cluster_size_for_device();
+    ClusterJob j = make_job(g, dims, a, b, iters, csize);
+    int rc = ensure_cluster_attrs();
+    if (rc) return rc;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = csize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(csize);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.dynamicSmemBytes = kClusterSmemMax + 128;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const ClusterJob *none = nullptr;
+    unsigned *noq = nullptr;
+    ST_CUDA(cudaLaunchKernelEx(&cfg, k_cluster, j, none, 1, noq));
+    if (res) *res = (iters & 1) ? b : a;
+    return STENCIL_OK;
+}
+
+// Whether a single grid is better served by one cluster than by the
+// full-GPU kernels: it fits in the cluster's shared memory.
+bool cluster_resident(const Geom &g, int dims) {
+    if (g.nx % 4 || g.radius < 1 || g.radius > 4) return false;
+    ClusterJob j = make_job(g, dims, nullptr, nullptr, 0, cluster_size_for_device());
+    return j.resident != 0;
+}
+
+
+
+// ---------------------------------------------------------------------------
+// Batch C ABI: a device job table + queue counter in a caller-provided
+// workspace, one persistent launch (capturable in a CUDA graph).
+// ---------------------------------------------------------------------------
+namespace {
+
+struct BatchHeader {
+    unsigned queue;
+    int njobs;
+    int cluster_size;
+    int clusters;
+};
+
+// Launch shape of each prepared workspace (set by prepare, read by launch).
+std::mutex g_batch_mu;
+std::vector<std::pair<const void *, BatchHeader>> g_batch;
+
+void remember(const void *ws, const BatchHeader &h) {
+    std::lock_guard<std::mutex> lock(g_batch_mu);
+    for (auto &c : g_batch)
+        if (c.first == ws) { c.second = h; return; }
+    g_batch.emplace_back(ws, h);
+}
+
+bool recall(const void *ws, BatchHeader *h) {
+    std::lock_guard<std::mutex> lock(g_batch_mu);
+    for (auto &c : g_batch)
+        if (c.first == ws) { *h = c.second; return true; }
+    return false;
+}
+
+size_t batch_bytes(int njobs) {
+    return ((sizeof(BatchHeader) + 255) & ~(size_t)255) + (size_t)njobs * sizeof(ClusterJob);
+}
+
+}  // namespace
+
+}  // namespace st
+
+using namespace st;
+
+extern "C" int stencil_batch_workspace_bytes(int njobs, size_t *bytes) {
+    if (njobs < 0 || !bytes) return fail(STENCIL_EINVAL, "bad arguments");
+    *bytes = batch_bytes(njobs);
+    return STENCIL_OK;
+}
+
+extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, int cluster_size,
+                                     void *d_workspace, size_t workspace_bytes,
+                                     stencil_stream_t stream) {
+    if (njobs < 0 || (njobs && !jobs) || !d_workspace)
+        return fail(STENCIL_EINVAL, "bad arguments");
+    if (workspace_bytes < batch_bytes(njobs))
+        return fail(STENCIL_EINVAL, "workspace too small: %zu < %zu bytes", workspace_bytes,
+                    batch_bytes(njobs));
+    if (reinterpret_cast<uintptr_t>(d_workspace) & 255)
+        return fail(STENCIL_EINVAL, "workspace must be 256-byte aligned");
+    if (cluster_size != 0 && cluster_size != 8 && cluster_size != 16)
+        return fail(STENCIL_EINVAL, "cluster_size must be 0, 8 or 16");
+    int rc0 = ensure_cluster_attrs();
+    if (rc0) return rc0;
+    const int csize = cluster_size ? cluster_size : cluster_size_for_device();
+    std::vector<ClusterJob> table;
+    std::vector<double> work;
+    table.reserve(njobs);
+    for (int i = 0; i < njobs; ++i) {
+        const stencil_batch_job &b = jobs[i];
+        stencil_params p;
+        stencil_params_init(&p);
+        p.dims = b.dims; p.nx = b.nx; p.ny = b.ny; p.nz = b.dims == 3 ? b.nz : 1;
+        p.radius = b.radius; p.iterations = b.iterations; p.mode = b.mode;
+        int rc = stencil_params_check(&p);
+        if (rc) return fail(rc, "job %d: %s", i, stencil_last_error());
+        if (!b.d_u1 || !b.d_u2 || b.d_u1 == b.d_u2 ||
+            ((reinterpret_cast<uintptr_t>(b.d_u1) | reinterpret_cast<uintptr_t>(b.d_u2)) & 15))
+            return fail(STENCIL_EINVAL, "job %d: two distinct 16-byte aligned buffers required", i);
+        if (!cluster_job_ok(b.dims, b.nx, b.ny, b.nz, b.radius))
+            return fail(STENCIL_EUNSUPPORTED, "job %d: batch jobs need nx %% 4 == 0 and radius <= 4", i);
+        table.push_back(make_job(make_geom(p), p.dims, b.d_u1, b.d_u2, b.iterations, csize));
+        work.push_back((double)cell_count(p) * b.iterations);
+    }
+    // Largest job first: the queue hands them out in this order.
+    std::vector<int> order(njobs);
+    for (int i = 0; i < njobs; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
+    std::vector<ClusterJob> sorted(njobs);
+    for (int i = 0; i < njobs; ++i) sorted[i] = table[order[i]];
+    BatchHeader h;
+    h.queue = 0;
+    h.njobs = njobs;
+    h.cluster_size = csize;
+    h.clusters = max_active_clusters(csize);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const size_t hb = (sizeof(BatchHeader) + 255) & ~(size_t)255;
+    char *ws = static_cast<char *>(d_workspace);
+    ST_CUDA(cudaMemcpyAsync(ws, &h, sizeof h, cudaMemcpyHostToDevice, s));
+    if (njobs)
+        ST_CUDA(cudaMemcpyAsync(ws + hb, sorted.data(), njobs * sizeof(ClusterJob),
+                                cudaMemcpyHostToDevice, s));
+    ST_CUDA(cudaStreamSynchronize(s));
+    remember(d_workspace, h);
+    return STENCIL_OK;
+}
+
+extern "C" int stencil_batch_launch(const void *d_workspace, stencil_stream_t stream) {
+    if (!d_workspace) return fail(STENCIL_EINVAL, "null workspace");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    BatchHeader h{};
+    if (!recall(d_workspace, &h))
+        return fail(STENCIL_EINVAL, "workspace was not prepared by stencil_batch_prepare");
+    if (h.njobs == 0) return STENCIL_OK;
+    const size_t hb = (sizeof(BatchHeader) + 255) & ~(size_t)255;
+    const ClusterJob *table = reinterpret_cast<const ClusterJob *>(static_cast<const char *>(d_workspace) + hb);
+    unsigned *queue = reinterpret_cast<unsigned *>(const_cast<void *>(d_workspace));
+    return launch_cluster_jobs(table, h.njobs, queue, std::min(h.clusters, h.njobs), h.cluster_size, s);
+}
+
+extern "C" int stencil_batch_forget(const void *d_workspace) {
+    std::lock_guard<std::mutex> lock(g_batch_mu);
+    for (size_t i = 0; i < g_batch.size(); ++i)
+        if (g_batch[i].first == d_workspace) {
+            g_batch.erase(g_batch.begin() + i);
+            break;
+        }
+    return STENCIL_OK;
+}

@@ -22,11 +22,10 @@
 // used by an updated cell.  Each input cell is read from HBM once per sweep;
 // halos of neighbouring tiles and chunks are re-read from L2.
 //
-// Work: the (tile, z-plane) steps in tile-major order are split into equal
-// contiguous shares, one per resident CTA; a share covers one or a few
-// (tile, z-range) segments.  The producer and the consumers walk the same
-// segments, and a monotone plane sequence number fixes each plane's slot and
-// mbarrier phase.  No CTA-wide
+// Work items are (tile, z-chunk) pairs, chunk-major so that co-resident CTAs
+// work on neighbouring tiles of one z range.  CTAs loop over items; the
+// producer and the consumers walk the same item sequence, and a monotone plane
+// sequence number fixes each plane's slot and mbarrier phase.  No CTA-wide
 // barrier is used after set-up, and every mbarrier wait is bounded.
 #include <algorithm>
 #include <cmath>
@@ -57,7 +56,7 @@ __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cas
 template <int R, int TX, int TY, int RY, int NS>
 __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <= 1 ? 2 : 1))
     k_stream3d(const __grid_constant__ CUtensorMap src_map, float *__restrict__ dst, Geom g,
-               int tiles_x, long long total) {
+               int tiles_x, int tiles_y, int zchunk, int items) {
     using S = StreamShape<R, TX, TY, RY, NS>;
     constexpr int C = 6 * R;  // 2*D*R with D = 3
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -75,22 +74,16 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
         fence_mbar_init();
     }
     __syncthreads();
-    // This CTA's share of the (tile, plane) steps: [lo, hi) in tile-major order.
-    const int zin = g.nz - 2 * R;
-    const long long lo = total * blockIdx.x / gridDim.x;
-    const long long hi = total * (blockIdx.x + 1) / gridDim.x;
+    const int ntiles = tiles_x * tiles_y;
 
     if (warp == S::CWARPS) {
         // ---------------- producer ----------------
         if (lane != 0) return;
         uint32_t q = 0;
-        for (long long i = lo; i < hi;) {
-            const int t = (int)(i / zin);
-            const int z0 = R + (int)(i - (long long)t * zin);
-            const long long rem_ = hi - (long long)t * zin;
-            const int z1 = R + (int)(rem_ < zin ? rem_ : (long long)zin);
-            i = (long long)t * zin + (z1 - R);
+        for (int item = blockIdx.x; item < items; item += gridDim.x) {
+            const int t = item % ntiles, ch = item / ntiles;
             const int x0 = (t % tiles_x) * TX, y0 = (t / tiles_x) * TY;
+            const int z0 = R + ch * zchunk, z1 = min(z0 + zchunk, g.nz - R);
             const int np = (z1 - z0) + 2 * R;
             for (int p = 0; p < np; ++p, ++q) {
                 const int s = q & (NS - 1);
@@ -112,14 +105,11 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
     };
     constexpr int QN = 2 * R + 1;
     float4 qz[RY][QN];  // z register queue, rotated by unrolling: plane z+k-R sits at index (z-z0+k) % QN
-    uint32_t qb = 0;    // sequence number of plane 0 of the current segment
-    for (long long i = lo; i < hi;) {
-        const int t = (int)(i / zin);
-        const int z0 = R + (int)(i - (long long)t * zin);
-        const long long rem_ = hi - (long long)t * zin;
-            const int z1 = R + (int)(rem_ < zin ? rem_ : (long long)zin);
-        i = (long long)t * zin + (z1 - R);
+    uint32_t qb = 0;    // sequence number of plane 0 of the current item
+    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+        const int t = item % ntiles, ch = item / ntiles;
         const int x0 = (t % tiles_x) * TX, y0 = (t / tiles_x) * TY;
+        const int z0 = R + ch * zchunk, z1 = min(z0 + zchunk, g.nz - R);
         const int np = (z1 - z0) + 2 * R;
         const int x = x0 + 4 * cx, ybase = y0 + cy * RY;
         const int own = (cy * RY + R) * S::PW + 4 * cx + S::RA;  // slot offset of row 0, cell 0
@@ -310,11 +300,27 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     const int tiles_x = (g.nx + k.tx - 1) / k.tx, tiles_y = (g.ny + k.ty - 1) / k.ty;
     const int tiles = tiles_x * tiles_y;
     const int zin = g.nz - 2 * R;
-    // Every resident CTA gets an equal contiguous share of the tile-major
-    // (tile, plane) steps: no partly filled last wave, and at most a few
-    // segments (each re-reads 2R halo planes) per CTA.
-    const long long total = (long long)tiles * zin;
-    const int grid = (int)std::min<long long>(resident, total);
+    // Items are (tile, z-chunk) pairs taken chunk-major, so CTAs running at
+    // the same time work on neighbouring tiles of one z range and their halo
+    // re-reads hit L2.  The chunk count is chosen so the items fill whole
+    // waves of resident CTAs (a partly filled last wave idles SMs) while
+    // chunks stay long (each re-reads 2R halo planes and re-primes the queue).
+    int nchunks = 1;
+    double best = 1e30;
+    for (int n = 1; n <= std::max(1, zin / 8); ++n) {
+        const int zc = (zin + n - 1) / n;
+        const long long it = (long long)tiles * ((zin + zc - 1) / zc);
+        const double waves = std::ceil((double)it / resident);
+        const double fill = (double)it / (waves * resident);  // <= 1
+        const double halo = 1.0 + 0.25 * (2.0 * R) / zc;      // halo planes mostly hit L2
+        const double cost = halo / fill + 0.002 * waves;       // small per-item overhead
+        if (cost < best - 1e-9) { best = cost; nchunks = n; }
+    }
+    int zchunk = (zin + nchunks - 1) / nchunks;
+    nchunks = (zin + zchunk - 1) / zchunk;
+    const int items = tiles * nchunks;
+    const int grid = std::min(items, resident);
+
     CUtensorMap maps[2];
     const long long dims[3] = {g.nx, g.ny, g.nz};
     const int box[3] = {k.tx + 2 * ((R + 3) & ~3), k.ty + 2 * R, 1};
@@ -324,10 +330,9 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     float *cur = a, *nxt = b;
     int ci = 0;
     Geom gg = g;
-    int tx_ = tiles_x;
-    long long tot_ = total;
+    int tx_ = tiles_x, ty_ = tiles_y, it_ = items;
     for (int it = 0; it < iters; ++it) {
-        void *args[] = {&maps[ci], &nxt, &gg, &tx_, &tot_};
+        void *args[] = {&maps[ci], &nxt, &gg, &tx_, &ty_, &zchunk, &it_};
         ST_CUDA(cudaLaunchKernel(k.fn, dim3(grid), dim3(k.threads), args, k.smem, s));
         std::swap(cur, nxt);
         ci ^= 1;

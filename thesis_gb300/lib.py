@@ -34,6 +34,15 @@ class StencilError(RuntimeError):
         super().__init__(msg)
 
 
+class BatchJob(ctypes.Structure):
+    _fields_ = [
+        ("d_u1", ctypes.c_void_p), ("d_u2", ctypes.c_void_p), ("dims", ctypes.c_int),
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("radius", ctypes.c_int), ("iterations", ctypes.c_int), ("mode", ctypes.c_int),
+        ("reserved", ctypes.c_int),
+    ]
+
+
 class StencilParams(ctypes.Structure):
     _fields_ = [
         ("dims", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int),
@@ -70,6 +79,10 @@ def load() -> ctypes.CDLL:
         "stencil_selftest_div": (i, [i, ctypes.POINTER(ctypes.c_ulonglong),
                                      ctypes.POINTER(ctypes.c_uint)]),
         "stencil_selftest_wait": (i, [i, ctypes.POINTER(i), ctypes.POINTER(i)]),
+        "stencil_batch_workspace_bytes": (i, [i, ctypes.POINTER(sz)]),
+        "stencil_batch_prepare": (i, [ctypes.POINTER(BatchJob), i, i, vp, sz, vp]),
+        "stencil_batch_launch": (i, [vp, vp]),
+        "stencil_batch_forget": (i, [vp]),
         "stencil_strerror": (ctypes.c_char_p, [i]),
         "stencil_last_error": (ctypes.c_char_p, []),
         "stencil_device_status": (i, [ctypes.POINTER(i)]),

@@ -157,3 +157,52 @@ def device_status() -> int:
     st = ctypes.c_int()
     _lib.check(_lib.load().stencil_device_status(ctypes.byref(st)), "stencil_device_status")
     return st.value
+
+
+class Batch:
+    """Many grids of uneven sizes and sweep counts in one persistent launch
+    (stencil_batch_prepare / stencil_batch_launch).
+
+    jobs: list of (d_u1, d_u2, radius, iterations, mode) with CUDA float32
+    tensors of shape (ny, nx) or (nz, ny, nx).  After ``launch`` each job's
+    result is in d_u1 for an even sweep count, else in d_u2 (``result(i)``).
+    """
+
+    def __init__(self, jobs, cluster_size: int = 0, stream=None):
+        import torch
+        self.jobs = list(jobs)
+        arr = (_lib.BatchJob * max(1, len(self.jobs)))()
+        for k, (u1, u2, radius, iters, mode) in enumerate(self.jobs):
+            _check_tensor(u1)
+            _check_tensor(u2, u1.shape)
+            j = arr[k]
+            j.d_u1, j.d_u2 = u1.data_ptr(), u2.data_ptr()
+            if u1.dim() == 2:
+                j.dims, j.ny, j.nx, j.nz = 2, u1.shape[0], u1.shape[1], 1
+            else:
+                j.dims, j.nz, j.ny, j.nx = 3, u1.shape[0], u1.shape[1], u1.shape[2]
+            j.radius, j.iterations, j.mode = radius, iters, mode
+        L = _lib.load()
+        nbytes = ctypes.c_size_t()
+        _lib.check(L.stencil_batch_workspace_bytes(len(self.jobs), ctypes.byref(nbytes)),
+                   "stencil_batch_workspace_bytes")
+        dev = self.jobs[0][0].device if self.jobs else torch.device("cuda")
+        self.workspace = torch.empty(nbytes.value + 256, dtype=torch.uint8, device=dev)
+        base = self.workspace.data_ptr()
+        self.ws = ctypes.c_void_p((base + 255) & ~255)
+        _lib.check(L.stencil_batch_prepare(arr, len(self.jobs), cluster_size, self.ws,
+                                           nbytes.value, _stream_handle(stream)),
+                   "stencil_batch_prepare")
+
+    def launch(self, stream=None):
+        _lib.check(_lib.load().stencil_batch_launch(self.ws, _stream_handle(stream)),
+                   "stencil_batch_launch")
+
+    def result(self, k):
+        u1, u2, _, iters, _ = self.jobs[k]
+        return u1 if iters % 2 == 0 else u2
+
+    def close(self):
+        if self.ws is not None:
+            _lib.load().stencil_batch_forget(self.ws)
+            self.ws = None
