@@ -117,6 +117,17 @@ STENCIL_API int stencil_init_reference(const stencil_params *p, float *d_u, sten
 /* count cells i.i.d. uniform [0,1): value(i) = (mix64(mix64(seed) + G*(i+1)) >> 40) * 2^-24,
  * mix64 = the SplitMix64 finaliser, G = 0x9E3779B97F4A7C15. */
 STENCIL_API int stencil_init_uniform(float *d_u, size_t count, uint64_t seed, stencil_stream_t stream);
+/* Border band: sum of `modes` (<= 16) smooth modes A cos(2 pi (a x/nx + b y/ny
+ * + c z/nz) + phi), a, b, c in {0..3}, A ~ N(0,1), phi ~ U[0, 2 pi); interior:
+ * uniform [0,1) as stencil_init_uniform(seed).  Parameters are drawn from
+ * `seed` on the host; values evaluated in double and rounded to float. */
+STENCIL_API int stencil_init_fourier(const stencil_params *p, float *d_u, uint64_t seed, int modes,
+                                     stencil_stream_t stream);
+/* 2-D Laplace borders: per edge, the linear interpolation of its two corner
+ * values (N(0,1)) plus sum_{k=1..K} A_k sin(pi k t), K ~ U{1..16}, A_k ~ N(0,1),
+ * t in [0,1] along the edge (continuous at the corners).  Interior zero. */
+STENCIL_API int stencil_init_laplace2d(const stencil_params *p, float *d_u, uint64_t seed,
+                                       stencil_stream_t stream);
 /* Copies the border band of src into dst (JACOBI set-up). */
 STENCIL_API int stencil_copy_border(const stencil_params *p, const float *d_src, float *d_dst,
                         stencil_stream_t stream);
@@ -150,6 +161,39 @@ STENCIL_API int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, 
 STENCIL_API int stencil_batch_launch(const void *d_workspace, stencil_stream_t stream);
 /* Drops the host-side record of a prepared workspace (call before freeing it). */
 STENCIL_API int stencil_batch_forget(const void *d_workspace);
+
+/* ---- Mixed-precision iterative refinement (no counterpart in the reference).
+ * Solves the JACOBI steady state in outer steps of inner_sweeps sweeps: the
+ * residual r = (M u + c) - u is recomputed in FP32 from the FP32 master grid
+ * d_u, the correction e of (I - M) e = r is swept in BF16 or FP16 storage
+ * with FP32 accumulation, and u += e.  In exact arithmetic the result after
+ * p->iterations sweeps is that of p->iterations plain sweeps.  With tol > 0
+ * the solve stops once the FP64 relative residual (computed on the GPU every
+ * check_every outer steps) drops below tol.  Needs p->mode == JACOBI and
+ * nx % 8 == 0; d_u's border band is never written.  Allocates nothing: the
+ * caller passes a 256-byte aligned workspace of stencil_ir_workspace_bytes. */
+enum { STENCIL_STORAGE_FP32 = 0, STENCIL_STORAGE_BF16 = 1, STENCIL_STORAGE_FP16 = 2 };
+
+typedef struct stencil_ir_params {
+    int storage;       /* STENCIL_STORAGE_BF16 or STENCIL_STORAGE_FP16 */
+    int inner_sweeps;  /* correction sweeps per outer step (0 = 50) */
+    int check_every;   /* outer steps between residual checks when tol > 0 */
+    int reserved[3];   /* must be zero */
+    double tol;        /* stop at this relative residual (0 = run all sweeps) */
+} stencil_ir_params;
+
+typedef struct stencil_ir_result {
+    int sweeps;          /* sweeps performed */
+    int outer_steps;     /* refinement steps performed */
+    double rel_residual; /* FP64 relative residual of the final u */
+} stencil_ir_result;
+
+STENCIL_API int stencil_ir_workspace_bytes(const stencil_params *p, const stencil_ir_params *ir,
+                                           size_t *bytes);
+/* Synchronises `stream` at each residual check and at the end. */
+STENCIL_API int stencil_ir_solve(const stencil_params *p, const stencil_ir_params *ir, float *d_u,
+                                 void *d_workspace, size_t workspace_bytes,
+                                 stencil_stream_t stream, stencil_ir_result *result);
 
 /* Relative residual ||b - A u||_2 / ||b||_2 of the steady state that JACOBI
  * iterates to, (A u)(x) = u(x) - mean of the 2*D*R axis neighbours over the

@@ -29,6 +29,13 @@ extern __device__ unsigned g_device_status;
 
 __device__ __forceinline__ void report_status(unsigned code) { atomicOr(&g_device_status, code); }
 
+// SplitMix64 finaliser (Steele, Lea & Flood 2014); identical to the oracle's.
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
 // ---------------------------------------------------------------------------
 // The per-cell update.  Order follows src/stencils.cu:8-19 with
 // src/stencil_accumulators.cu:6-16: axes i, j, k; on each axis the offsets

@@ -40,7 +40,7 @@ struct ClusterJob {
     int radius, iters, legacy, resident;
 };
 
-constexpr int kClusterThreads = 256;
+constexpr int kClusterThreads = 512;
 
 __device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 

@@ -1,0 +1,319 @@
+// k_ir.cu -- mixed-precision iterative refinement for the JACOBI steady state.
+//
+// The Jacobi sweep u' = M u + c (M = mean of the 2*D*R axis neighbours over
+// the update region, c = the border contributions) is split into outer steps
+// of m sweeps.  Each outer step:
+//   1. r = (M u + c) - u from the FP32 master u (FP32 arithmetic), scaled by a
+//      power of two s so that |r/s| <= 1, stored in BF16 or FP16;
+//   2. e_1 = r/s (the first correction sweep from e_0 = 0), then m-1 sweeps
+//      e_{j+1} = M e_j + r/s with e stored in BF16/FP16 and every sum
+//      accumulated in FP32 (the border band of e and r is zero);
+//   3. u += s * e_m in FP32.
+// In exact arithmetic u + s*e_m is exactly m Jacobi sweeps from u, so the
+// total sweep count means the same as for the FP32 loop; only rounding
+// differs.  The FP64 relative residual (k_util.cu) decides convergence when a
+// tolerance is given.  Correction sweeps move 6 bytes per cell update (read e
+// and r, write e) instead of 8.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+
+#include "host.hpp"
+
+namespace st {
+
+size_t residual_scratch_bytes();
+int launch_residual(const Geom &g, int dims, const float *u, double *scratch, cudaStream_t s);
+
+template <typename E>
+struct LowP;
+template <>
+struct LowP<__nv_bfloat16> {
+    __device__ static float2 to2(uint32_t w) {
+        return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&w));
+    }
+    __device__ static uint32_t from2(float a, float b) {
+        __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        return *reinterpret_cast<uint32_t *>(&h);
+    }
+    __device__ static float to(const __nv_bfloat16 v) { return __bfloat162float(v); }
+    __device__ static __nv_bfloat16 from(float v) { return __float2bfloat16_rn(v); }
+};
+template <>
+struct LowP<__half> {
+    __device__ static float2 to2(uint32_t w) {
+        return __half22float2(*reinterpret_cast<const __half2 *>(&w));
+    }
+    __device__ static uint32_t from2(float a, float b) {
+        __half2 h = __floats2half2_rn(a, b);
+        return *reinterpret_cast<uint32_t *>(&h);
+    }
+    __device__ static float to(const __half v) { return __half2float(v); }
+    __device__ static __half from(float v) { return __float2half_rn(v); }
+};
+
+template <typename E>
+__device__ __forceinline__ void unpack8(const uint4 &q, float *f) {
+    const float2 a = LowP<E>::to2(q.x), b = LowP<E>::to2(q.y), c = LowP<E>::to2(q.z),
+                 d = LowP<E>::to2(q.w);
+    f[0] = a.x; f[1] = a.y; f[2] = b.x; f[3] = b.y; f[4] = c.x; f[5] = c.y; f[6] = d.x; f[7] = d.y;
+}
+
+// One correction sweep e_out = M e + rhs on 8-cell vectors (nx % 8 == 0).
+template <typename E, int D, int R>
+__global__ void __launch_bounds__(256)
+    k_lp_sweep(const E *__restrict__ e, E *__restrict__ eo, const E *__restrict__ rhs, Geom g) {
+    constexpr int C = 2 * D * R;
+    const int nv = g.nx >> 3;
+    const long long nrows = (long long)(g.ny - 2 * R) * (D == 3 ? g.nz - 2 * R : 1);
+    const long long total = nrows * nv;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int v = (int)(t % nv);
+        const long long rr = t / nv;
+        const int j = R + (int)(rr % (g.ny - 2 * R));
+        const int k = D == 3 ? R + (int)(rr / (g.ny - 2 * R)) : 0;
+        const int x0 = v * 8;
+        if (x0 + 7 < R || x0 >= g.nx - R) continue;
+        const long long row = (long long)j * g.sy + (long long)k * g.sz;
+        const uint4 *src = reinterpret_cast<const uint4 *>(e + row);
+        float w[24];
+        {
+            const uint4 z4 = make_uint4(0, 0, 0, 0);
+            unpack8<E>(v > 0 ? __ldg(src + v - 1) : z4, w);
+            unpack8<E>(__ldg(src + v), w + 8);
+            unpack8<E>(v + 1 < nv ? __ldg(src + v + 1) : z4, w + 16);
+        }
+        float acc[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[c] = 0.0f;
+#pragma unroll
+        for (int o = -R; o <= R; ++o) {
+            if (!o) continue;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) acc[c] += w[8 + c + o];
+        }
+#pragma unroll
+        for (int o = -R; o <= R; ++o) {
+            if (!o) continue;
+            float f[8];
+            unpack8<E>(__ldg(reinterpret_cast<const uint4 *>(e + row + o * g.sy) + v), f);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) acc[c] += f[c];
+        }
+        if (D == 3) {
+#pragma unroll
+            for (int o = -R; o <= R; ++o) {
+                if (!o) continue;
+                float f[8];
+                unpack8<E>(__ldg(reinterpret_cast<const uint4 *>(e + row + o * g.sz) + v), f);
+#pragma unroll
+                for (int c = 0; c < 8; ++c) acc[c] += f[c];
+            }
+        }
+        float rf[8];
+        unpack8<E>(__ldg(reinterpret_cast<const uint4 *>(rhs + row) + v), rf);
+        float out[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) out[c] = div_coeff<C>(acc[c]) + rf[c];
+        E *dst = eo + row + x0;
+        if (x0 >= R && x0 + 7 < g.nx - R) {
+            uint4 q;
+            q.x = LowP<E>::from2(out[0], out[1]);
+            q.y = LowP<E>::from2(out[2], out[3]);
+            q.z = LowP<E>::from2(out[4], out[5]);
+            q.w = LowP<E>::from2(out[6], out[7]);
+            *reinterpret_cast<uint4 *>(dst) = q;
+        } else {
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                if (in_range(x0 + c, g.nx, R)) dst[c] = LowP<E>::from(out[c]);
+        }
+    }
+}
+
+// r = (M u + c) - u over the update region (FP32).  pass 0: max |r| into
+// *max_bits.  pass 1: stores r * 2^-ceil(log2 max) in E and the scale in *scale.
+template <typename E, int D, int R>
+__global__ void __launch_bounds__(256)
+    k_ir_resid(const float *__restrict__ u, E *__restrict__ r, Geom g, unsigned *max_bits,
+               float *scale, int pass) {
+    constexpr int C = 2 * D * R;
+    float inv = 1.0f;
+    if (pass == 1) {
+        const float m = __uint_as_float(*max_bits);
+        int ex = 0;
+        if (m > 0.0f) frexpf(m, &ex);  // m = f * 2^ex, f in [0.5, 1)
+        const float s = ldexpf(1.0f, ex);
+        inv = 1.0f / s;
+        if (blockIdx.x == 0 && threadIdx.x == 0) *scale = s;
+    }
+    float local = 0.0f;
+    const long long n = (long long)(g.nx - 2 * R) * (g.ny - 2 * R) * (D == 3 ? g.nz - 2 * R : 1);
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = R + (int)(c % (g.nx - 2 * R));
+        const long long q = c / (g.nx - 2 * R);
+        const int j = R + (int)(q % (g.ny - 2 * R));
+        const int k = D == 3 ? R + (int)(q / (g.ny - 2 * R)) : 0;
+        const long long idx = i + (long long)j * g.sy + (long long)k * g.sz;
+        float acc = 0.0f;
+#pragma unroll
+        for (int o = -R; o <= R; ++o)
+            if (o) acc += u[idx + o];
+#pragma unroll
+        for (int o = -R; o <= R; ++o)
+            if (o) acc += u[idx + o * g.sy];
+        if (D == 3) {
+#pragma unroll
+            for (int o = -R; o <= R; ++o)
+                if (o) acc += u[idx + o * g.sz];
+        }
+        const float res = div_coeff<C>(acc) - u[idx];
+        if (pass == 0) local = fmaxf(local, fabsf(res));
+        else r[idx] = LowP<E>::from(res * inv);
+    }
+    if (pass == 0) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) local = fmaxf(local, __shfl_xor_sync(0xffffffffu, local, o));
+        if ((threadIdx.x & 31) == 0) atomicMax(max_bits, __float_as_uint(local));
+    }
+}
+
+// u += s * e over the update region.
+template <typename E, int D, int R>
+__global__ void __launch_bounds__(256)
+    k_ir_update(float *__restrict__ u, const E *__restrict__ e, Geom g, const float *scale) {
+    const float s = *scale;
+    const long long n = (long long)(g.nx - 2 * R) * (g.ny - 2 * R) * (D == 3 ? g.nz - 2 * R : 1);
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = R + (int)(c % (g.nx - 2 * R));
+        const long long q = c / (g.nx - 2 * R);
+        const int j = R + (int)(q % (g.ny - 2 * R));
+        const int k = D == 3 ? R + (int)(q / (g.ny - 2 * R)) : 0;
+        const long long idx = i + (long long)j * g.sy + (long long)k * g.sz;
+        u[idx] = fmaf(s, LowP<E>::to(e[idx]), u[idx]);
+    }
+}
+
+namespace {
+
+template <typename E, int D, int R>
+int ir_loop(const stencil_params &p, const stencil_ir_params &ir, float *u, char *ws,
+            cudaStream_t s, stencil_ir_result *out) {
+    const Geom g = make_geom(p);
+    const size_t n = (size_t)cell_count(p);
+    const size_t lp_bytes = (n * sizeof(E) + 255) & ~(size_t)255;
+    E *r = reinterpret_cast<E *>(ws);
+    E *ea = reinterpret_cast<E *>(ws + lp_bytes);
+    E *eb = reinterpret_cast<E *>(ws + 2 * lp_bytes);
+    unsigned *max_bits = reinterpret_cast<unsigned *>(ws + 3 * lp_bytes);
+    float *scale = reinterpret_cast<float *>(ws + 3 * lp_bytes + 4);
+    double *resid = reinterpret_cast<double *>(ws + 3 * lp_bytes + 256);
+    // Border bands of r and e stay zero for the whole solve.
+    ST_CUDA(cudaMemsetAsync(ws, 0, 3 * lp_bytes, s));
+    const int blocks = 4 * num_sms();
+    const int m_inner = ir.inner_sweeps > 0 ? ir.inner_sweeps : 50;
+    int done = 0, outer = 0;
+    double rel = -1.0;
+    while (done < p.iterations) {
+        const int m = std::min(m_inner, p.iterations - done);
+        ST_CUDA(cudaMemsetAsync(max_bits, 0, sizeof(unsigned), s));
+        k_ir_resid<E, D, R><<<blocks, 256, 0, s>>>(u, r, g, max_bits, scale, 0);
+        k_ir_resid<E, D, R><<<blocks, 256, 0, s>>>(u, r, g, max_bits, scale, 1);
+        ST_CUDA(cudaGetLastError());
+        ST_CUDA(cudaMemcpyAsync(ea, r, n * sizeof(E), cudaMemcpyDeviceToDevice, s));
+        E *cur = ea, *nxt = eb;
+        for (int it = 1; it < m; ++it) {
+            k_lp_sweep<E, D, R><<<8 * num_sms(), 256, 0, s>>>(cur, nxt, r, g);
+            std::swap(cur, nxt);
+        }
+        ST_CUDA(cudaGetLastError());
+        k_ir_update<E, D, R><<<blocks, 256, 0, s>>>(u, cur, g, scale);
+        ST_CUDA(cudaGetLastError());
+        done += m;
+        ++outer;
+        const bool last = done >= p.iterations;
+        if ((ir.tol > 0.0 && (ir.check_every <= 1 || outer % ir.check_every == 0)) || last) {
+            int rc = launch_residual(g, p.dims, u, resid, s);
+            if (rc) return rc;
+            double sums[2];
+            const size_t off = residual_scratch_bytes() / sizeof(double) - 2;
+            ST_CUDA(cudaMemcpyAsync(sums, resid + off, sizeof sums, cudaMemcpyDeviceToHost, s));
+            ST_CUDA(cudaStreamSynchronize(s));
+            rel = sums[1] > 0.0 ? sqrt(sums[0]) / sqrt(sums[1]) : sqrt(sums[0]);
+            if (ir.tol > 0.0 && rel < ir.tol) break;
+        }
+    }
+    if (out) {
+        out->sweeps = done;
+        out->outer_steps = outer;
+        out->rel_residual = rel;
+    }
+    return STENCIL_OK;
+}
+
+template <typename E>
+int ir_dispatch(const stencil_params &p, const stencil_ir_params &ir, float *u, char *ws,
+                cudaStream_t s, stencil_ir_result *out) {
+    const int key = p.dims * 10 + p.radius;
+    switch (key) {
+        case 21: return ir_loop<E, 2, 1>(p, ir, u, ws, s, out);
+        case 22: return ir_loop<E, 2, 2>(p, ir, u, ws, s, out);
+        case 24: return ir_loop<E, 2, 4>(p, ir, u, ws, s, out);
+        case 31: return ir_loop<E, 3, 1>(p, ir, u, ws, s, out);
+        case 32: return ir_loop<E, 3, 2>(p, ir, u, ws, s, out);
+        case 34: return ir_loop<E, 3, 4>(p, ir, u, ws, s, out);
+        default: return fail(STENCIL_EUNSUPPORTED, "IR has no D=%d R=%d instance", p.dims, p.radius);
+    }
+}
+
+size_t ir_bytes(const stencil_params &p, int storage) {
+    const size_t n = (size_t)cell_count(p);
+    const size_t esz = storage == STENCIL_STORAGE_FP32 ? 4 : 2;
+    const size_t lp = (n * esz + 255) & ~(size_t)255;
+    return 3 * lp + 256 + residual_scratch_bytes();
+}
+
+}  // namespace
+}  // namespace st
+
+using namespace st;
+
+extern "C" int stencil_ir_workspace_bytes(const stencil_params *p, const stencil_ir_params *ir,
+                                          size_t *bytes) {
+    int rc = stencil_params_check(p);
+    if (rc) return rc;
+    if (!ir || !bytes) return fail(STENCIL_EINVAL, "null pointer");
+    *bytes = ir_bytes(*p, ir->storage);
+    return STENCIL_OK;
+}
+
+extern "C" int stencil_ir_solve(const stencil_params *p, const stencil_ir_params *ir, float *d_u,
+                                void *d_workspace, size_t workspace_bytes,
+                                stencil_stream_t stream, stencil_ir_result *result) {
+    int rc = stencil_params_check(p);
+    if (rc) return rc;
+    if (!ir || !d_u || !d_workspace) return fail(STENCIL_EINVAL, "null pointer");
+    if (p->mode != STENCIL_MODE_JACOBI)
+        return fail(STENCIL_EINVAL, "iterative refinement solves the JACOBI steady state");
+    if (ir->storage != STENCIL_STORAGE_BF16 && ir->storage != STENCIL_STORAGE_FP16)
+        return fail(STENCIL_EINVAL, "storage must be STENCIL_STORAGE_BF16 or STENCIL_STORAGE_FP16");
+    if (ir->inner_sweeps < 0 || ir->check_every < 0 || ir->tol < 0.0)
+        return fail(STENCIL_EINVAL, "inner_sweeps, check_every and tol must be >= 0");
+    for (int r : ir->reserved)
+        if (r) return fail(STENCIL_EINVAL, "reserved fields must be zero");
+    if (p->nx % 8) return fail(STENCIL_EUNSUPPORTED, "IR needs nx %% 8 == 0");
+    if (workspace_bytes < ir_bytes(*p, ir->storage))
+        return fail(STENCIL_EINVAL, "workspace too small (%zu < %zu bytes)", workspace_bytes,
+                    ir_bytes(*p, ir->storage));
+    if ((reinterpret_cast<uintptr_t>(d_workspace) & 255) || (reinterpret_cast<uintptr_t>(d_u) & 15))
+        return fail(STENCIL_EINVAL, "workspace must be 256-byte and u 16-byte aligned");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    char *ws = static_cast<char *>(d_workspace);
+    if (ir->storage == STENCIL_STORAGE_BF16)
+        return ir_dispatch<__nv_bfloat16>(*p, *ir, d_u, ws, s, result);
+    return ir_dispatch<__half>(*p, *ir, d_u, ws, s, result);
+}

@@ -8,13 +8,6 @@ namespace st {
 
 __device__ unsigned g_device_status = 0;
 
-// SplitMix64 finaliser (Steele, Lea & Flood 2014); identical to the oracle's.
-__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
-
 __global__ void k_init_uniform(float *__restrict__ u, size_t count, uint64_t seed) {
     const uint64_t base = mix64(seed);
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count;

@@ -43,6 +43,20 @@ class BatchJob(ctypes.Structure):
     ]
 
 
+class IrParams(ctypes.Structure):
+    _fields_ = [("storage", ctypes.c_int), ("inner_sweeps", ctypes.c_int),
+                ("check_every", ctypes.c_int), ("reserved", ctypes.c_int * 3),
+                ("tol", ctypes.c_double)]
+
+
+class IrResult(ctypes.Structure):
+    _fields_ = [("sweeps", ctypes.c_int), ("outer_steps", ctypes.c_int),
+                ("rel_residual", ctypes.c_double)]
+
+
+STORAGE_FP32, STORAGE_BF16, STORAGE_FP16 = 0, 1, 2
+
+
 class StencilParams(ctypes.Structure):
     _fields_ = [
         ("dims", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int),
@@ -74,6 +88,8 @@ def load() -> ctypes.CDLL:
         "stencil_init_reference": (i, [P, vp, vp]),
         "stencil_init_uniform": (i, [vp, sz, u64, vp]),
         "stencil_copy_border": (i, [P, vp, vp, vp]),
+        "stencil_init_fourier": (i, [P, vp, u64, i, vp]),
+        "stencil_init_laplace2d": (i, [P, vp, u64, vp]),
         "stencil_residual": (i, [P, vp, ctypes.POINTER(ctypes.c_double), vp]),
         "stencil_residual_noalloc": (i, [P, vp, ctypes.POINTER(ctypes.c_double), vp]),
         "stencil_selftest_div": (i, [i, ctypes.POINTER(ctypes.c_ulonglong),
@@ -83,6 +99,9 @@ def load() -> ctypes.CDLL:
         "stencil_batch_prepare": (i, [ctypes.POINTER(BatchJob), i, i, vp, sz, vp]),
         "stencil_batch_launch": (i, [vp, vp]),
         "stencil_batch_forget": (i, [vp]),
+        "stencil_ir_workspace_bytes": (i, [P, ctypes.POINTER(IrParams), ctypes.POINTER(sz)]),
+        "stencil_ir_solve": (i, [P, ctypes.POINTER(IrParams), vp, vp, sz, vp,
+                                 ctypes.POINTER(IrResult)]),
         "stencil_strerror": (ctypes.c_char_p, [i]),
         "stencil_last_error": (ctypes.c_char_p, []),
         "stencil_device_status": (i, [ctypes.POINTER(i)]),

@@ -118,6 +118,28 @@ def init_uniform(shape, seed: int, device="cuda", stream=None):
     return u
 
 
+def init_fourier(shape, seed: int, radius: int, modes: int = 8, device="cuda", stream=None):
+    """Smooth Fourier-mode border band + uniform [0,1) interior (stencil_init_fourier)."""
+    import torch
+    u = torch.empty(shape, dtype=torch.float32, device=device)
+    p = _lib.make_params(shape, radius, 0)
+    _lib.check(_lib.load().stencil_init_fourier(ctypes.byref(p), ctypes.c_void_p(u.data_ptr()),
+                                                seed, modes, _stream_handle(stream)),
+               "stencil_init_fourier")
+    return u
+
+
+def init_laplace2d(shape, seed: int, device="cuda", stream=None):
+    """2-D Laplace Dirichlet border (continuous, Fourier modes per edge), zero interior."""
+    import torch
+    u = torch.empty(shape, dtype=torch.float32, device=device)
+    p = _lib.make_params(shape, 1, 0)
+    _lib.check(_lib.load().stencil_init_laplace2d(ctypes.byref(p), ctypes.c_void_p(u.data_ptr()),
+                                                  seed, _stream_handle(stream)),
+               "stencil_init_laplace2d")
+    return u
+
+
 def copy_border(src, dst, radius: int, stream=None):
     _check_tensor(src)
     _check_tensor(dst, src.shape)
@@ -206,3 +228,27 @@ class Batch:
         if self.ws is not None:
             _lib.load().stencil_batch_forget(self.ws)
             self.ws = None
+
+
+def ir_solve(d_u, radius: int, iterations: int, storage: str = "bf16", inner_sweeps: int = 0,
+             tol: float = 0.0, check_every: int = 1, workspace=None, stream=None):
+    """Mixed-precision iterative refinement in place on the FP32 master d_u
+    (stencil_ir_solve).  Returns (sweeps, outer_steps, rel_residual)."""
+    import torch
+    _check_tensor(d_u)
+    p = _lib.make_params(tuple(d_u.shape), radius, iterations, _lib.MODE_JACOBI)
+    ir = _lib.IrParams()
+    ir.storage = {"bf16": _lib.STORAGE_BF16, "fp16": _lib.STORAGE_FP16}[storage]
+    ir.inner_sweeps, ir.check_every, ir.tol = inner_sweeps, check_every, tol
+    L = _lib.load()
+    nbytes = ctypes.c_size_t()
+    _lib.check(L.stencil_ir_workspace_bytes(ctypes.byref(p), ctypes.byref(ir), ctypes.byref(nbytes)),
+               "stencil_ir_workspace_bytes")
+    if workspace is None or workspace.numel() < nbytes.value + 256:
+        workspace = torch.empty(nbytes.value + 256, dtype=torch.uint8, device=d_u.device)
+    ws = (workspace.data_ptr() + 255) & ~255
+    res = _lib.IrResult()
+    _lib.check(L.stencil_ir_solve(ctypes.byref(p), ctypes.byref(ir), ctypes.c_void_p(d_u.data_ptr()),
+                                  ctypes.c_void_p(ws), nbytes.value, _stream_handle(stream),
+                                  ctypes.byref(res)), "stencil_ir_solve")
+    return res.sweeps, res.outer_steps, res.rel_residual
