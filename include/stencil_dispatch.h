@@ -149,7 +149,8 @@ typedef struct stencil_batch_job {
 STENCIL_API int stencil_batch_workspace_bytes(int njobs, size_t *bytes);
 /* Validates the jobs, orders them largest first and writes the job table into
  * d_workspace (256-byte aligned, caller-owned).  cluster_size: CTAs per
- * cluster (8 or 16; 0 = the largest the device schedules).  Synchronises
+ * cluster (1, 2, 4, 8 or 16; 0 = the largest the device schedules; 1 suits
+ * many small grids, each then swept by one CTA).  Synchronises
  * `stream`. */
 STENCIL_API int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, int cluster_size,
                                       void *d_workspace, size_t workspace_bytes,

@@ -83,7 +83,10 @@ def test_borders_generators(cuda):
     assert np.array_equal(a, b) and np.isfinite(a).all()
     inner = a[2:-2, 2:-2, 2:-2]
     assert inner.min() >= 0 and inner.max() < 1
-    lap = S.init_laplace2d((64, 80), 3).cpu().numpy()
+    lap = S.init_laplace2d((2048, 2048), 3).cpu().numpy()
     assert np.all(lap[1:-1, 1:-1] == 0)
-    # continuous at the corners: neighbours along both edges are close to the corner value
-    assert abs(lap[0, 1] - lap[0, 0]) < 1.0 and abs(lap[1, 0] - lap[0, 0]) < 1.0
+    # continuous at the corners: on a fine grid the cells next to a corner
+    # along both edges are close to the corner value
+    for (j, i), (dj, di) in [((0, 0), (1, 1)), ((0, -1), (1, -1)), ((-1, 0), (-1, 1)), ((-1, -1), (-1, -1))]:
+        c = lap[j, i]
+        assert abs(lap[j, i + di] - c) < 0.5 and abs(lap[j + dj, i] - c) < 0.5

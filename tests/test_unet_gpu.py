@@ -1,0 +1,136 @@
+"""U-Net kernels (BF16 tensor cores, FP32 accumulate) against torch CPU
+references: each operator, then the whole network's loss and gradients."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf16_round(a):
+    import torch
+    return torch.as_tensor(a).to(torch.bfloat16).to(torch.float64)
+
+
+def _nhwc_to_nchw(t):
+    return t.permute(0, 3, 1, 2)
+
+
+@pytest.mark.parametrize("cin,cout,h,w", [(32, 64, 16, 24), (64, 32, 8, 8), (96, 32, 12, 20),
+                                          (384, 128, 8, 16)])
+def test_conv3x3_fwd_dgrad_wgrad(cuda, cin, cout, h, w):
+    import torch
+    from thesis_gb300 import unet as U
+    L = U._L()
+    g = torch.Generator().manual_seed(cin + cout)
+    n = 2
+    x = torch.randn(n, h, w, cin, generator=g).to(torch.bfloat16)
+    wt = (torch.randn(cout, 9, cin, generator=g) * 0.1).to(torch.bfloat16)
+    b = torch.randn(cout, generator=g).float()
+    dy = torch.randn(n, h, w, cout, generator=g).to(torch.bfloat16)
+    xd, wd, bd, dyd = x.cuda(), wt.cuda(), b.cuda(), dy.cuda()
+    y = torch.empty(n, h, w, cout, dtype=torch.bfloat16, device="cuda")
+    U._chk(L.unet_conv3x3_fwd(ctypes.byref(U.view(xd)), U._p(wd), U._p(bd), ctypes.byref(U.view(y)), 1, None), "fwd")
+    # reference in float64 on the same BF16 inputs
+    X = _nhwc_to_nchw(x.double()).requires_grad_(True)
+    W = wt.double().reshape(cout, 3, 3, cin).permute(0, 3, 1, 2).contiguous().requires_grad_(True)
+    pre = torch.nn.functional.conv2d(X, W, b.double(), padding=1)
+    Y = torch.relu(pre)
+    got = _nhwc_to_nchw(y.cpu().double())
+    err = (got - Y).abs().max().item() / Y.abs().max().item()
+    assert err < 1e-2, err
+    # data gradient through the flipped weights; weight gradient
+    wflip = torch.empty(cin, 9, cout, dtype=torch.bfloat16, device="cuda")
+    U._chk(L.unet_flip_weights(U._p(wd), U._p(wflip), cout, cin, None), "flip")
+    dx = torch.empty(n, h, w, cin, dtype=torch.bfloat16, device="cuda")
+    U._chk(L.unet_conv3x3_fwd(ctypes.byref(U.view(dyd)), U._p(wflip), None, ctypes.byref(U.view(dx)), 0, None), "dgrad")
+    dw = torch.zeros(cout, 9, cin, device="cuda")
+    db = torch.zeros(cout, device="cuda")
+    U._chk(L.unet_conv3x3_wgrad(ctypes.byref(U.view(xd)), ctypes.byref(U.view(dyd)), U._p(dw), U._p(db), None), "wgrad")
+    pre.backward(_nhwc_to_nchw(dy.double()))
+    gx = _nhwc_to_nchw(dx.cpu().double())
+    assert (gx - X.grad).abs().max().item() / X.grad.abs().max().item() < 1e-2
+    gw = dw.cpu().double().reshape(cout, 3, 3, cin).permute(0, 3, 1, 2)
+    assert (gw - W.grad).abs().max().item() / W.grad.abs().max().item() < 1e-4
+    gb = _nhwc_to_nchw(dy.double()).sum((0, 2, 3))
+    assert (db.cpu().double() - gb).abs().max().item() / gb.abs().max().item() < 1e-4
+
+
+def test_pool_upsample_relu_add_head(cuda):
+    import torch
+    from thesis_gb300 import unet as U
+    L = U._L()
+    g = torch.Generator().manual_seed(3)
+    x = torch.randn(2, 8, 12, 32, generator=g).to(torch.bfloat16).cuda()
+    y = torch.empty(2, 4, 6, 32, dtype=torch.bfloat16, device="cuda")
+    U._chk(L.unet_maxpool2_fwd(ctypes.byref(U.view(x)), ctypes.byref(U.view(y)), None), "pool")
+    X = _nhwc_to_nchw(x.cpu().double()).requires_grad_(True)
+    P = torch.nn.functional.max_pool2d(X, 2)
+    assert torch.equal(_nhwc_to_nchw(y.cpu().double()), P)
+    dy = torch.randn(2, 4, 6, 32, generator=g).to(torch.bfloat16).cuda()
+    dx = torch.empty_like(x)
+    U._chk(L.unet_maxpool2_bwd(ctypes.byref(U.view(x)), ctypes.byref(U.view(y)), ctypes.byref(U.view(dy)),
+                               ctypes.byref(U.view(dx)), None), "pool bwd")
+    P.backward(_nhwc_to_nchw(dy.cpu().double()))
+    assert torch.equal(_nhwc_to_nchw(dx.cpu().double()), X.grad)
+    up = torch.empty(2, 16, 24, 32, dtype=torch.bfloat16, device="cuda")
+    U._chk(L.unet_upsample2_fwd(ctypes.byref(U.view(x)), ctypes.byref(U.view(up)), None), "up")
+    ref = torch.nn.functional.interpolate(_nhwc_to_nchw(x.cpu().double()), scale_factor=2, mode="nearest")
+    assert torch.equal(_nhwc_to_nchw(up.cpu().double()), ref)
+    gup = torch.randn(2, 16, 24, 32, generator=g).to(torch.bfloat16).cuda()
+    gx = torch.empty_like(x)
+    U._chk(L.unet_upsample2_bwd(ctypes.byref(U.view(gup)), ctypes.byref(U.view(gx)), None), "up bwd")
+    want = _nhwc_to_nchw(gup.cpu().double()).reshape(2, 32, 8, 2, 12, 2).sum((3, 5))
+    assert (_nhwc_to_nchw(gx.cpu().double()) - want).abs().max().item() < 0.05
+    # head
+    hw = torch.randn(32, generator=g).float().cuda()
+    hb = torch.tensor([0.25], device="cuda")
+    out = torch.empty(2, 8, 12, device="cuda")
+    U._chk(L.unet_head_fwd(ctypes.byref(U.view(x)), U._p(hw), U._p(hb), U._p(out), None), "head")
+    ref = (x.cpu().double() * hw.cpu().double()).sum(-1) + 0.25
+    assert (out.cpu().double() - ref).abs().max().item() < 1e-4
+
+
+def test_network_gradients_match_cpu_reference(cuda):
+    """Loss and every parameter gradient of the BF16 network vs torch float64."""
+    import torch
+    from oracle import unet_ref as R
+    from thesis_gb300 import stencil as S, unet as U
+    n, h, w = 2, 32, 32
+    fields = torch.stack([S.init_laplace2d((h, w), 100 + k) for k in range(n)])
+    target = torch.randn(n, h, w, device="cuda") * 0.1
+    net = U.UNet(seed=7)
+    net.zero_grad()
+    B = net.loss_and_grad(fields, target)
+    net.backward(B)
+    torch.cuda.synchronize()
+    loss_gpu = B["loss"].item()
+    # reference
+    x, coons = R.features(fields.cpu().numpy())
+    params = {}
+    for name, _, _ in R.LAYERS:
+        wb = net.params[name]["wb"].cpu().double().requires_grad_(True)
+        bb = net.params[name]["b"].cpu().double().requires_grad_(True)
+        params[name] = (wb, bb)
+    hw = net.head["w"].cpu().double().requires_grad_(True)
+    hb = net.head["b"].cpu().double().requires_grad_(True)
+    X = _bf16_round(x)
+    out = R.forward(torch, params, X, hw, hb)
+    loss = R.masked_mse(torch, out, torch.from_numpy(coons), target.cpu().double())
+    loss.backward()
+    # the library accumulates the sum of squares; the reference returns the mean
+    assert loss_gpu / (n * (h - 2) * (w - 2)) == pytest.approx(loss.item(), rel=5e-2)
+    worst = 0.0
+    for name, _, _ in R.LAYERS:
+        for k, ref in (("dw", params[name][0].grad), ("db", params[name][1].grad)):
+            got = net.params[name][k].cpu().double()
+            if k == "dw":
+                ref = ref.reshape(got.shape)
+            rel = (got - ref).norm().item() / max(ref.norm().item(), 1e-30)
+            worst = max(worst, rel)
+            assert rel < 0.1, (name, k, rel)
+    print("worst normwise gradient error %.3e" % worst)
+    for k, ref in (("dw", hw.grad), ("db", hb.grad)):
+        got = net.head[k].cpu().double()
+        assert (got - ref).norm().item() / max(ref.norm().item(), 1e-30) < 0.1

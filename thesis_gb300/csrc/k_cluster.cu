@@ -456,8 +456,8 @@ extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, i
                     batch_bytes(njobs));
     if (reinterpret_cast<uintptr_t>(d_workspace) & 255)
         return fail(STENCIL_EINVAL, "workspace must be 256-byte aligned");
-    if (cluster_size != 0 && cluster_size != 8 && cluster_size != 16)
-        return fail(STENCIL_EINVAL, "cluster_size must be 0, 8 or 16");
+    if (cluster_size < 0 || cluster_size > 16 || (cluster_size & (cluster_size - 1)))
+        return fail(STENCIL_EINVAL, "cluster_size must be 0 or a power of two <= 16");
     int rc0 = ensure_cluster_attrs();
     if (rc0) return rc0;
     const int csize = cluster_size ? cluster_size : cluster_size_for_device();
