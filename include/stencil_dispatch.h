@@ -238,6 +238,17 @@ STENCIL_API int stencil_selftest_div(int coeff, unsigned long long *mismatches,
                                      unsigned *first_mismatch);
 STENCIL_API int stencil_selftest_wait(int limit_ms, int *completed, int *status);
 
+/* ---- Tuning table consulted by STENCIL_VARIANT_AUTO (filled by the
+ * project's autotuner, thesis_gb300/autotune.py; no counterpart in the
+ * reference, whose tuner rebuilt the binary per configuration).  An entry
+ * maps (dims, radius, the smallest power of two >= the largest extent) to a
+ * variant and its tuning fields (block_*, coarsen_x, temporal) taken from
+ * `choice`; setting an existing key replaces it.  At most 256 entries. */
+STENCIL_API int stencil_tuning_set(const stencil_params *key, const stencil_params *choice);
+/* Looks up the entry for key; returns STENCIL_EINVAL if there is none. */
+STENCIL_API int stencil_tuning_get(const stencil_params *key, stencil_params *choice);
+STENCIL_API int stencil_tuning_clear(void);
+
 /* Frees every workspace this library holds on the current device. */
 STENCIL_API int stencil_release(void);
 

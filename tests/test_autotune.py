@@ -1,0 +1,79 @@
+"""The project's autotuner: search space, optimiser (against brute force on
+synthetic scores, as the reference tuner's own self-tests did with fake
+evaluators), the JSON database and the library's tuning table."""
+import ctypes
+import itertools
+import json
+import os
+import tempfile
+
+import pytest
+
+from thesis_gb300 import autotune as A
+from thesis_gb300 import lib as L
+
+
+def test_block_filter_matches_reference_constraints():
+    shapes = A.block_shapes(3)
+    assert (32, 2, 2) in shapes and (32, 8, 4) in shapes  # reference defaults / heuristic
+    for bx, by, bz in shapes:
+        assert 32 <= bx * by * bz <= 1024 and bx >= by >= bz and bx >= 8
+    assert all(bz == 1 for _, _, bz in A.block_shapes(2))
+
+
+def test_coordinate_descent_finds_separable_optimum():
+    space = {"a": list(range(6)), "b": list(range(5)), "c": [1, 2, 4, 8]}
+    target = {"a": 4, "b": 1, "c": 8}
+    score = lambda cfg: sum((cfg[k] - target[k]) ** 2 for k in target) + 1.0
+    best, s, n = A.coordinate_descent({"a": 0, "b": 0, "c": 1}, space, score)
+    brute = min((dict(zip(space, v)) for v in itertools.product(*space.values())), key=score)
+    assert best == brute == target and s == 1.0
+    assert n < 6 * 5 * 4  # fewer evaluations than brute force
+
+
+def test_optimise_picks_variant_then_its_parameters():
+    top = [{"variant": "x"}, {"variant": "y", "k": 3}]
+    sub = {"y": {"k": [1, 2, 3, 4, 5]}}
+    score = lambda c: 10.0 if c["variant"] == "x" else abs(c["k"] - 2) + 1.0
+    best, s, _ = A.optimise(top, sub, score)
+    assert best == {"variant": "y", "k": 2} and s == 1.0
+
+
+def test_infinite_score_is_never_chosen():
+    top = [{"variant": "broken"}, {"variant": "ok"}]
+    best, s, _ = A.optimise(top, {}, lambda c: float("inf") if c["variant"] == "broken" else 2.0)
+    assert best["variant"] == "ok"
+
+
+def test_tuning_table_and_db_round_trip(stencil_lib):
+    stencil_lib.stencil_tuning_clear()
+    entry = {"dims": 3, "radius": 1, "shape": [100, 100, 96], "bucket": 128,
+             "choice": {"variant": "smem_padded", "block": [32, 4, 2], "coarsen_x": 8}}
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "db.json")
+        A.save_db(path, [entry], "test")
+        A.load_db(path)
+    key = L.make_params((120, 128, 128), 1, 0)  # same (dims, radius, bucket 128)
+    out = L.StencilParams()
+    assert stencil_lib.stencil_tuning_get(ctypes.byref(key), ctypes.byref(out)) == 0
+    assert out.variant == L.VARIANT_SMEM_PADDED and (out.block_x, out.block_y, out.block_z) == (32, 4, 2)
+    assert out.coarsen_x == 8
+    other = L.make_params((300, 300, 300), 1, 0)  # bucket 512: no entry
+    assert stencil_lib.stencil_tuning_get(ctypes.byref(other), ctypes.byref(out)) == L.EINVAL
+    stencil_lib.stencil_tuning_clear()
+    assert stencil_lib.stencil_tuning_get(ctypes.byref(key), ctypes.byref(out)) == L.EINVAL
+
+
+@pytest.mark.gpu
+def test_tune_on_gpu_and_auto_uses_it(cuda):
+    import numpy as np
+    import torch
+    from thesis_gb300 import stencil as S
+    entry = A.tune((64, 64, 128), 1, sweeps=5, repeats=1, log=None)
+    assert entry["us_per_sweep"] > 0 and entry["candidates"] >= 3
+    A.install(entry)
+    u = S.init_uniform((64, 64, 128), 3)
+    got = S.sweep(u.clone(), u.clone(), 1, 7, L.MODE_JACOBI, "auto").cpu().numpy()
+    want = S.sweep(u.clone(), u.clone(), 1, 7, L.MODE_JACOBI, "base").cpu().numpy()
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    L.load().stencil_tuning_clear()

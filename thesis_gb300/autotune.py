@@ -1,0 +1,231 @@
+"""Autotuner for the sweep kernels; replaces the reference's Python-2
+Autotuning harness (Autotuning/tuner/*.py driven by
+scripts/autotune_configuration.py), which rebuilt and re-ran one binary per
+configuration and scored it by the last line of its output.
+
+Here every candidate runs in-process through the C ABI:
+  * the search space follows the reference's (block sizes in powers of two
+    with 32 <= bx*by*bz <= 1024 and bx >= by >= bz, bx >= 8,
+    Autotuning/tuner/optimisation.py:150-160; coarsening factors; radius and
+    size from the workload), extended with this library's variants, stream
+    tile shapes and cluster sizes;
+  * the optimiser is a two-level variable tree, as the reference's
+    independence tree (Autotuning/tuner/vartree.py): the variant is chosen
+    first, each with its default parameters, then the winner's own
+    parameters are refined by coordinate descent;
+  * a candidate is accepted only if its output is bit-identical to the base
+    variant's on a short run (all variants keep the reference summation
+    order), and it is scored by the minimum over repeats of CUDA-event time
+    per sweep (the reference kept min/median/mean of `repeat` runs,
+    Autotuning/tuner/evaluator.py);
+  * results go to a JSON database (dims, radius, size bucket) -> choice,
+    which load_db() installs into the library (stencil_tuning_set) so that
+    STENCIL_VARIANT_AUTO uses it.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import itertools
+import json
+import os
+import time
+
+from . import lib as _lib
+
+BLOCK_VALUES = [1, 2, 4, 8, 16, 32, 64, 128, 256]
+
+
+def block_shapes(dims: int):
+    """The reference's block filter (Autotuning/tuner/optimisation.py:150-160)."""
+    out = []
+    for bx, by, bz in itertools.product(BLOCK_VALUES, BLOCK_VALUES, BLOCK_VALUES if dims == 3 else [1]):
+        n = bx * by * bz
+        if 32 <= n <= 1024 and bx >= by >= bz and bx >= 8:
+            out.append((bx, by, bz))
+    return out
+
+
+def variant_space(shape, radius):
+    """Variants with their default parameters, then each variant's own
+    parameter lists (the second level of the tree)."""
+    dims = len(shape)
+    nx = shape[-1]
+    top = [{"variant": "base"}]
+    sub = {"base": {"block": block_shapes(dims), "coarsen_x": [4, 8, 16]}}
+    if nx % 4 == 0:
+        top.append({"variant": "smem_padded"})
+        sub["smem_padded"] = {"block": [b for b in block_shapes(dims) if b[0] <= 64]}
+        if dims == 3 and radius <= 4:
+            top.append({"variant": "smem_register"})
+            sub["smem_register"] = {"block": [(0, 0, 0), (16, 32, 1)]}  # 128 x 16 or 64 x 32 tiles
+        if radius <= 4:
+            top.append({"variant": "cluster"})
+            sub["cluster"] = {}
+    return top, sub
+
+
+def coordinate_descent(start: dict, space: dict, score, max_rounds: int = 3):
+    """Minimises score(config) over the variables of `space`, one variable at
+    a time, until a full round changes nothing."""
+    best = dict(start)
+    best_s = score(best)
+    tried = {json.dumps(best, sort_keys=True): best_s}
+    for _ in range(max_rounds):
+        changed = False
+        for var, values in space.items():
+            for v in values:
+                cand = dict(best)
+                cand[var] = v
+                key = json.dumps(cand, sort_keys=True)
+                if key not in tried:
+                    tried[key] = score(cand)
+                if tried[key] < best_s:
+                    best, best_s, changed = cand, tried[key], True
+        if not changed:
+            break
+    return best, best_s, len(tried)
+
+
+def optimise(top, sub, score):
+    """Two-level tree: best variant at its defaults, then its own parameters."""
+    scored = [(score(c), c) for c in top]
+    scored.sort(key=lambda t: t[0])
+    first_s, first = scored[0]
+    space = sub.get(first["variant"], {})
+    best, best_s, n = coordinate_descent(first, space, score) if space else (first, first_s, 0)
+    return best, best_s, len(top) + n
+
+
+class GpuEvaluator:
+    """Times candidates on the current GPU; rejects any that changes results."""
+
+    def __init__(self, shape, radius, sweeps=20, repeats=3, seed=1):
+        import torch
+        from . import stencil as S
+        self.S, self.torch = S, torch
+        self.shape, self.radius, self.sweeps, self.repeats = tuple(shape), radius, sweeps, repeats
+        self.u0 = S.init_uniform(self.shape, seed)
+        a, b = self.u0.clone(), self.u0.clone()
+        self.ref = S.sweep(a, b, radius, 3, _lib.MODE_JACOBI, "base").clone()
+        self.a, self.b = self.u0.clone(), self.u0.clone()
+
+    def params(self, cfg):
+        return _lib.make_params(self.shape, self.radius, 0, _lib.MODE_JACOBI, cfg["variant"],
+                                tuple(cfg.get("block", (0, 0, 0))), cfg.get("coarsen_x", 0),
+                                cfg.get("temporal", 0))
+
+    def __call__(self, cfg) -> float:
+        S, torch = self.S, self.torch
+        try:
+            a, b = self.u0.clone(), self.u0.clone()
+            out = S.dispatch(self._with_iters(cfg, 3), a, b)
+            if not torch.equal(out.view(torch.int32), self.ref.view(torch.int32)):
+                return float("inf")
+            best = float("inf")
+            for _ in range(self.repeats):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                S.dispatch(self._with_iters(cfg, self.sweeps), self.a, self.b)
+                e1.record()
+                e1.synchronize()
+                best = min(best, e0.elapsed_time(e1) / 1e3 / self.sweeps)
+            return best
+        except _lib.StencilError:
+            return float("inf")
+
+    def _with_iters(self, cfg, iters):
+        p = self.params(cfg)
+        p.iterations = iters
+        return p
+
+
+def tune(shape, radius, sweeps=20, repeats=3, log=print):
+    top, sub = variant_space(shape, radius)
+    ev = GpuEvaluator(shape, radius, sweeps, repeats)
+    t0 = time.time()
+    best, best_s, n = optimise(top, sub, ev)
+    entry = {"dims": len(shape), "radius": radius, "shape": list(shape),
+             "bucket": 1 << (max(shape) - 1).bit_length(), "choice": best,
+             "us_per_sweep": best_s * 1e6, "candidates": n, "tune_s": time.time() - t0}
+    if log:
+        log(json.dumps(entry))
+    return entry
+
+
+def install(entry):
+    """Puts one database entry into the library's tuning table."""
+    shape = tuple(entry["shape"])
+    key = _lib.make_params(shape, entry["radius"], 0)
+    c = entry["choice"]
+    choice = _lib.make_params(shape, entry["radius"], 0, _lib.MODE_JACOBI, c["variant"],
+                              tuple(c.get("block", (0, 0, 0))), c.get("coarsen_x", 0),
+                              c.get("temporal", 0))
+    _lib.check(_lib.load().stencil_tuning_set(ctypes.byref(key), ctypes.byref(choice)),
+               "stencil_tuning_set")
+
+
+def load_db(path):
+    with open(path) as f:
+        db = json.load(f)
+    for e in db.get("entries", []):
+        install(e)
+    return db
+
+
+def save_db(path, entries, device=""):
+    db = {"version": 1, "device": device, "entries": entries}
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(db, f, indent=1)
+    os.replace(tmp, path)
+
+
+def tune_batch_cluster_size(make_jobs, sizes=(1, 2, 4, 8, 16), log=print):
+    """Chooses the cluster size of a batched launch by timing it: make_jobs()
+    returns fresh (d_u1, d_u2, radius, iterations, mode) jobs."""
+    import torch
+    from . import stencil as S
+    best, best_t = None, float("inf")
+    for c in sizes:
+        jobs = make_jobs()
+        try:
+            bt = S.Batch(jobs, cluster_size=c)
+        except _lib.StencilError:
+            continue
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        bt.launch()
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        bt.close()
+        if log:
+            log("cluster_size %d: %.3f s" % (c, t))
+        if t < best_t:
+            best, best_t = c, t
+    return best, best_t
+
+
+def main():
+    ap = argparse.ArgumentParser(description="tune the sweep kernels for one workload")
+    ap.add_argument("--shape", type=int, nargs="+", required=True)
+    ap.add_argument("--radius", type=int, default=1)
+    ap.add_argument("--sweeps", type=int, default=20)
+    ap.add_argument("--db", default="tuning.json")
+    args = ap.parse_args()
+    import torch
+    from . import build
+    build.build()
+    entries = []
+    if os.path.exists(args.db):
+        entries = json.load(open(args.db)).get("entries", [])
+    e = tune(args.shape, args.radius, args.sweeps)
+    entries = [x for x in entries if not (x["dims"] == e["dims"] and x["radius"] == e["radius"]
+                                          and x["bucket"] == e["bucket"])] + [e]
+    save_db(args.db, entries, torch.cuda.get_device_name())
+
+
+if __name__ == "__main__":
+    main()

@@ -162,6 +162,32 @@ static int ws_scratch(int dev, size_t bytes, void **out) {
     return STENCIL_OK;
 }
 
+// Tuning table (stencil_tuning_set): (dims, radius, size bucket) -> choice.
+struct TuneEntry {
+    int dims, radius, bucket;
+    stencil_params choice;
+};
+static std::mutex g_tune_mu;
+static std::vector<TuneEntry> g_tune;
+
+static int size_bucket(const stencil_params &p) {
+    int m = std::max(p.nx, std::max(p.ny, p.dims == 3 ? p.nz : 1));
+    int b = 1;
+    while (b < m) b <<= 1;
+    return b;
+}
+
+static bool tuned_choice(const stencil_params &p, stencil_params *out) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    const int b = size_bucket(p);
+    for (const TuneEntry &e : g_tune)
+        if (e.dims == p.dims && e.radius == p.radius && e.bucket == b) {
+            *out = e.choice;
+            return true;
+        }
+    return false;
+}
+
 // Variant choice when the caller leaves it to the library: grids that fit a
 // cluster's shared memory run all sweeps in one cluster launch (launch- and
 // sync-bound otherwise); large 3-D grids stream; the rest use the base kernel.
@@ -225,7 +251,20 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
     float *cur = d_u1, *nxt = d_u2;
     if (d_result) *d_result = cur;
     if (p->iterations == 0) return STENCIL_OK;
-    int variant = p->variant == STENCIL_VARIANT_AUTO ? choose_variant(*p) : p->variant;
+    int variant = p->variant;
+    stencil_params tuned;
+    if (variant == STENCIL_VARIANT_AUTO && tuned_choice(*p, &tuned)) {
+        // The tuned variant and tuning fields replace the caller's zeros.
+        stencil_params q = *p;
+        q.variant = tuned.variant;
+        if (!q.block_x) q.block_x = tuned.block_x;
+        if (!q.block_y) q.block_y = tuned.block_y;
+        if (!q.block_z) q.block_z = tuned.block_z;
+        if (!q.coarsen_x) q.coarsen_x = tuned.coarsen_x;
+        if (!q.temporal) q.temporal = tuned.temporal;
+        if (q.variant != STENCIL_VARIANT_AUTO) return stencil_dispatch_ex(&q, d_u1, d_u2, stream, d_result);
+    }
+    if (variant == STENCIL_VARIANT_AUTO) variant = choose_variant(*p);
     if (variant == STENCIL_VARIANT_SMEM_REGISTER && !(p->dims == 3 && stream3d_supported(g)))
         variant = STENCIL_VARIANT_SMEM_PADDED;
     if ((variant == STENCIL_VARIANT_SMEM || variant == STENCIL_VARIANT_SMEM_PADDED) &&
@@ -340,6 +379,41 @@ int stencil_residual(const stencil_params *p, const float *d_u, double *rel_resi
         ST_CUDA(cudaStreamSynchronize(s));
         *rel_residual = sums[1] > 0.0 ? sqrt(sums[0]) / sqrt(sums[1]) : sqrt(sums[0]);
     }
+    return STENCIL_OK;
+}
+
+int stencil_tuning_set(const stencil_params *key, const stencil_params *choice) {
+    int rc = stencil_params_check(key);
+    if (rc) return rc;
+    if (!choice) return fail(STENCIL_EINVAL, "null choice");
+    stencil_params c = *choice;
+    c.dims = key->dims; c.nx = key->nx; c.ny = key->ny; c.nz = key->nz;
+    c.radius = key->radius; c.iterations = key->iterations; c.mode = key->mode;
+    rc = stencil_params_check(&c);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    const int b = size_bucket(*key);
+    for (TuneEntry &e : g_tune)
+        if (e.dims == key->dims && e.radius == key->radius && e.bucket == b) {
+            e.choice = c;
+            return STENCIL_OK;
+        }
+    if (g_tune.size() >= 256) return fail(STENCIL_EINVAL, "tuning table full (256 entries)");
+    g_tune.push_back({key->dims, key->radius, b, c});
+    return STENCIL_OK;
+}
+
+int stencil_tuning_get(const stencil_params *key, stencil_params *choice) {
+    int rc = stencil_params_check(key);
+    if (rc) return rc;
+    if (!choice) return fail(STENCIL_EINVAL, "null choice");
+    if (!tuned_choice(*key, choice)) return fail(STENCIL_EINVAL, "no tuning entry for this key");
+    return STENCIL_OK;
+}
+
+int stencil_tuning_clear(void) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune.clear();
     return STENCIL_OK;
 }
 

@@ -102,6 +102,9 @@ def load() -> ctypes.CDLL:
         "stencil_ir_workspace_bytes": (i, [P, ctypes.POINTER(IrParams), ctypes.POINTER(sz)]),
         "stencil_ir_solve": (i, [P, ctypes.POINTER(IrParams), vp, vp, sz, vp,
                                  ctypes.POINTER(IrResult)]),
+        "stencil_tuning_set": (i, [P, P]),
+        "stencil_tuning_get": (i, [P, P]),
+        "stencil_tuning_clear": (i, []),
         "stencil_strerror": (ctypes.c_char_p, [i]),
         "stencil_last_error": (ctypes.c_char_p, []),
         "stencil_device_status": (i, [ctypes.POINTER(i)]),
