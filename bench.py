@@ -50,6 +50,10 @@ def parse():
     ap.add_argument("--no-r4", action="store_true", help="skip the radius-4 line item")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the 2-D, precision and batching line items")
+    ap.add_argument("--learned", action="store_true",
+                    help="also run the learned-warm-start workload (several minutes)")
     return ap.parse_args()
 
 
@@ -303,6 +307,17 @@ def run_ours(args):
 
     out["clocks"] = clk.summary()
 
+    # ---- the other workloads, each as its own line item ---------------------
+    if not args.no_configs and rank == 0:
+        out["configs"] = {}
+        out["configs"]["c1_2d_256"] = bench_c1(S, lib, torch)
+        out["configs"]["c3_precision_768"] = bench_c3(S, lib, torch)
+        out["configs"]["c4_batch_512"] = bench_c4(S, lib, torch)
+        if args.learned:
+            from thesis_gb300 import warmstart as W
+            seeds = list(range(10_000_000, 10_000_256))
+            out["configs"]["c5_learned_512"] = bench_c5(W, torch, seeds)
+
     # ---- CPU baseline: the oracle on the host cores, bounded sample -----------
     if not args.no_cpu and rank == 0:
         out["cpu_baseline"] = cpu_baseline(u0.cpu().numpy(), args.radius, target_s=10.0)
@@ -312,6 +327,161 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def _events(torch):
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def bench_c1(S, lib, torch, steps=5):
+    """2-D 256^2 R=1, 1000 Jacobi sweeps: the whole loop in one cluster launch."""
+    shape, R, sweeps = (256, 256), 1, 1000
+    u0 = S.init_uniform(shape, SEED)
+    a, b = u0.clone(), u0.clone()
+    for _ in range(3):
+        S.sweep(a, b, R, sweeps, lib.MODE_JACOBI, "auto")
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        a.copy_(u0)
+        e0, e1 = _events(torch)
+        e0.record()
+        S.sweep(a, b, R, sweeps, lib.MODE_JACOBI, "auto")
+        e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    ups = 254.0 * 254.0 * sweeps
+    import numpy as np
+    from oracle import oracle as O
+    h = u0.cpu().numpy()
+    t0 = time.perf_counter()
+    O.run(h.copy(), h.copy(), R, O.JACOBI, sweeps, 1)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "2D 256^2 FP32 R=1 Jacobi, 1000 sweeps (one cluster launch, grid resident in DSMEM)",
+            "value": round(ups / min(times) / 1e9, 3), "unit": "GCell-updates/s",
+            "ms_per_solve": round(min(times) * 1e3, 4), "us_per_sweep": round(min(times) / sweeps * 1e6, 3),
+            "bound": "latency (cluster barrier per sweep); 512 KiB working set is on-chip",
+            "cpu_baseline": {"value": round(ups / cpu_s / 1e9, 3), "unit": "GCell-updates/s",
+                             "cores": 1, "kind": "port",
+                             "sample": "full workload, oracle single-threaded like stencil_cpu"}}
+
+
+def bench_c3(S, lib, torch):
+    """3-D 768^3 R=4, 2000 sweeps: FP32 loop vs mixed-precision refinement."""
+    shape, R, sweeps = (768, 768, 768), 4, 2000
+    ups = 760.0 ** 3 * sweeps
+    u0 = S.init_fourier(shape, SEED, R, modes=8)
+    res = {"workload": "3D 768^3 R=4, 2000 sweeps; Fourier border (8 modes) + uniform interior",
+           "unit": "GCell-updates/s"}
+    a, b = u0.clone(), u0.clone()
+    S.sweep(a, b, R, 20, lib.MODE_JACOBI, "auto")
+    a.copy_(u0)
+    e0, e1 = _events(torch)
+    e0.record()
+    fp32 = S.sweep(a, b, R, sweeps, lib.MODE_JACOBI, "auto")
+    e1.record()
+    e1.synchronize()
+    t32 = e0.elapsed_time(e1) / 1e3
+    res["fp32"] = {"value": round(ups / t32 / 1e9, 2), "s": round(t32, 3),
+                   "rel_residual": S.residual(fp32, R),
+                   "roofline_frac": round(ups / t32 * 8 / 1e9 / peaks()[0], 4)}
+    fp32 = fp32.clone()
+    del a, b
+    ws = None
+    for st in ("bf16", "fp16"):
+        u = u0.clone()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        done, outer, rel = S.ir_solve(u, R, sweeps, st, inner_sweeps=50)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        err = float((u - fp32).abs().max() / fp32.abs().max())
+        res["ir_" + st] = {"value": round(ups / t / 1e9, 2), "s": round(t, 3), "rel_residual": rel,
+                           "normwise_err_vs_fp32": err, "speedup_vs_fp32": round(t32 / t, 3),
+                           "bytes_per_update": 6}
+        del u
+    torch.cuda.empty_cache()
+    return res
+
+
+def c4_jobs(seed=20251204):
+    """384 2-D R=1 grids (side log-uniform [64, 2048]) and 128 3-D R=2 grids
+    (side log-uniform [32, 256]), sweeps uniform [100, 5000]; sides rounded to
+    multiples of 4 (the batched kernels read 16-byte vectors)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(384):
+        s = int(round(np.exp(rng.uniform(np.log(64), np.log(2048))) / 4)) * 4
+        specs.append(((s, s), 1, int(rng.integers(100, 5001))))
+    for _ in range(128):
+        s = int(round(np.exp(rng.uniform(np.log(32), np.log(256))) / 4)) * 4
+        specs.append(((s, s, s), 2, int(rng.integers(100, 5001))))
+    return specs
+
+
+def bench_c4(S, lib, torch):
+    """512 grids of uneven sizes and sweep counts in one persistent launch,
+    captured in a CUDA graph; cluster size picked by the autotuner."""
+    from thesis_gb300 import autotune as A
+    specs = c4_jobs()
+    ups = 0.0
+    for shape, R, it in specs:
+        n = 1.0
+        for d in shape:
+            n *= d - 2 * R
+        ups += n * it
+    grids = []
+    for k, (shape, R, it) in enumerate(specs):
+        u = S.init_uniform(shape, SEED + k)
+        grids.append((u, u.clone()))
+
+    def sample_jobs():
+        # every 8th grid, sweeps / 10: a proxy of the batch for the tuner
+        return [(grids[k][0], grids[k][1], specs[k][1], max(10, specs[k][2] // 10), lib.MODE_JACOBI)
+                for k in range(0, len(specs), 8)]
+
+    csize, _ = A.tune_batch_cluster_size(sample_jobs, log=None)
+    jobs = [(g[0], g[1], sp[1], sp[2], lib.MODE_JACOBI) for g, sp in zip(grids, specs)]
+    bt = S.Batch(jobs, cluster_size=csize)
+    stream = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        bt.launch(stream=stream)  # warm-up
+        stream.synchronize()
+        with torch.cuda.graph(graph, stream=stream):
+            bt.launch(stream=stream)
+    times = []
+    for _ in range(3):
+        e0, e1 = _events(torch)
+        e0.record(stream)
+        graph.replay()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    bt.close()
+    mem = sum(g[0].numel() * 8 for g in grids)
+    del grids, jobs
+    torch.cuda.empty_cache()
+    return {"workload": "512 grids: 384 2D R=1 side 64..2048 + 128 3D R=2 side 32..256, 100..5000 sweeps",
+            "value": round(ups / min(times) / 1e9, 2), "unit": "GCell-updates/s",
+            "s_per_batch": round(min(times), 3), "cell_updates": ups, "cluster_size": csize,
+            "device_bytes": mem, "launches_per_batch": 1, "graph": True,
+            "roofline_frac_if_hbm": round(ups / min(times) * 8 / 1e9 / peaks()[0], 4)}
+
+
+def bench_c5(W, torch, seeds):
+    from thesis_gb300.unet import UNet
+    t0 = time.time()
+    fields, sols = W.generate_pairs(20000, 128, sweeps=40000)
+    gen_s = time.time() - t0
+    net = UNet(seed=0)
+    losses, train_s = W.train(net, fields, sols, epochs=24, batch=64)
+    del fields, sols
+    torch.cuda.empty_cache()
+    res = W.evaluate(net, seeds, 512, 1e-5, log=lambda *a: None)
+    res.update({"pairs": 20000, "gen_s": gen_s, "train_s": train_s, "final_loss": losses[-1]})
+    return res
 
 
 def cpu_baseline(host_grid, radius, target_s=10.0, threads=None):
