@@ -452,13 +452,14 @@ def bench_c4(S, lib, torch):
         with torch.cuda.graph(graph, stream=stream):
             bt.launch(stream=stream)
     times = []
-    for _ in range(3):
-        e0, e1 = _events(torch)
-        e0.record(stream)
-        graph.replay()
-        e1.record(stream)
-        e1.synchronize()
-        times.append(e0.elapsed_time(e1) / 1e3)
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            e0, e1 = _events(torch)
+            e0.record(stream)
+            graph.replay()  # replays on the current stream
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
     bt.close()
     mem = sum(g[0].numel() * 8 for g in grids)
     del grids, jobs

@@ -1,0 +1,65 @@
+"""Small, self-contained runs of each hot kernel, for profilers.
+
+  python -m thesis_gb300.profile_cases <case>
+
+Each case warms up, then runs the kernel a few more times; sizes are chosen so
+that the working set exceeds the 129 MB L2 where the kernel is HBM-bound, yet a
+full ncu capture of one launch ends in seconds.
+"""
+import sys
+import time
+
+
+def main(case):
+    import torch
+    from . import build, lib, stencil as S
+    build.build()
+    J = lib.MODE_JACOBI
+    if case in ("stream_r1", "stream_r4"):
+        R = 1 if case == "stream_r1" else 4
+        u = S.init_uniform((320, 320, 320), 1)  # 131 MB per buffer
+        a, b = u.clone(), u.clone()
+        for _ in range(4):
+            S.sweep(a, b, R, 2, J, "smem_register")
+    elif case == "base_r1":
+        u = S.init_uniform((320, 320, 320), 1)
+        a, b = u.clone(), u.clone()
+        for _ in range(4):
+            S.sweep(a, b, 1, 2, J, "base")
+    elif case == "cluster_2d256":
+        u = S.init_uniform((256, 256), 1)
+        a, b = u.clone(), u.clone()
+        for _ in range(4):
+            S.sweep(a, b, 1, 1000, J, "cluster")
+    elif case == "lp_sweep_r4":
+        u = S.init_fourier((384, 384, 384), 1, 4)
+        for _ in range(2):
+            S.ir_solve(u, 4, 8, "bf16", inner_sweeps=8)
+    elif case == "unet_train":
+        from .unet import UNet
+        from . import warmstart as W
+        fields = W.borders(range(64), 128)
+        target = W.coons_fill(fields)
+        net = UNet(seed=0)
+        for _ in range(3):
+            net.zero_grad()
+            B = net.loss_and_grad(fields, target)
+            net.backward(B)
+            net.adam_step()
+    elif case == "batch_small":
+        jobs = []
+        for k in range(64):
+            n = 64 + 32 * (k % 8)
+            u = S.init_uniform((n, n), k)
+            jobs.append((u, u.clone(), 1, 200 + 10 * k, J))
+        bt = S.Batch(jobs)
+        for _ in range(3):
+            bt.launch()
+    else:
+        raise SystemExit("unknown case " + case)
+    torch.cuda.synchronize()
+    print("done", case)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1])
