@@ -196,6 +196,8 @@ def evaluate(net, seeds, size=512, tol=1e-5, chunk=2000, log=print):
     torch.cuda.synchronize()
     t0 = time.time()
     for mode in ("direct", "coarse"):
+        predict(net, f, mode)  # warm-up: allocates the activation buffers for this shape
+        torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         p = predict(net, f, mode)
