@@ -161,3 +161,32 @@ def test_full_size_512_cubed(cuda, radius):
         torch.cuda.empty_cache()
     assert bits_equal(outs["base"], outs["smem_register"])
     assert bits_equal(outs["base"], outs["auto"])
+
+
+TB_CASES = [((64, 64, 64), 1, 2, 8), ((64, 64, 64), 1, 3, 9), ((64, 64, 64), 1, 4, 13),
+            ((40, 52, 100), 1, 4, 11), ((30, 36, 48), 2, 2, 7), ((12, 12, 12), 1, 4, 8),
+            ((9, 20, 136), 1, 4, 4), ((100, 70, 260), 2, 2, 4)]
+
+
+@pytest.mark.parametrize("case", TB_CASES, ids=lambda c: "x".join(map(str, c[0])) + "_r%d_T%d_i%d" % c[1:])
+def test_temporal_blocking_matches_oracle(cuda, case):
+    """COOP: T sweeps per HBM pass with overlapped tiles, bit-exact with the oracle."""
+    shape, radius, T, iters = case
+    u = O.uniform(shape, seed=17)
+    got, *_ = gpu_run(u, radius, iters, O.JACOBI, "coop", temporal=T)
+    assert bits_equal(got, oracle_run(u, radius, iters, O.JACOBI))
+
+
+@pytest.mark.slow
+def test_temporal_blocking_full_size(cuda):
+    """512^3: the temporally blocked passes equal the single-sweep kernel bit for bit."""
+    import torch
+    from thesis_gb300 import stencil as S
+    u = S.init_uniform((512, 512, 512), 99)
+    outs = []
+    for variant, T in (("smem_register", 0), ("coop", 4), ("coop", 3)):
+        a, b = u.clone(), u.clone()
+        outs.append(S.sweep(a, b, 1, 24, O.JACOBI, variant, temporal=T).cpu().numpy())
+        del a, b
+        torch.cuda.empty_cache()
+    assert bits_equal(outs[0], outs[1]) and bits_equal(outs[0], outs[2])

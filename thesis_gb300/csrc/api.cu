@@ -19,6 +19,7 @@ size_t residual_scratch_bytes();
 int launch_residual(const Geom &g, int dims, const float *u, double *scratch, cudaStream_t s);
 bool stream3d_supported(const Geom &g);
 bool tile_supported(const Geom &g, int dims);
+bool tb3d_supported(const Geom &g);
 
 static thread_local char t_err[512];
 
@@ -281,6 +282,14 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
             return STENCIL_OK;
         }
         variant = STENCIL_VARIANT_COOP;
+    }
+    if (variant == STENCIL_VARIANT_COOP && p->dims == 3 && tb3d_supported(g) &&
+        p->temporal != 1) {
+        float *res = nullptr;
+        rc = run_tb3d(g, cur, nxt, p->iterations, p->temporal, s, &res);
+        if (rc) return rc;
+        if (d_result) *d_result = res;
+        return STENCIL_OK;
     }
     if (variant == STENCIL_VARIANT_COOP)
         variant = p->dims == 3 && stream3d_supported(g) ? STENCIL_VARIANT_SMEM_REGISTER
