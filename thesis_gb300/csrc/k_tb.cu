@@ -35,7 +35,7 @@ struct TbShape {
     static constexpr int PLANE_BYTES = PLANE_FLOATS * 4;
     static constexpr int NR = 2 * R + 1;      // ring of levels 1..T-1
     static constexpr int NS = 2 * R + 1 + 3;  // level-0 ring: window + 3 in flight
-    static constexpr int CONSUMERS = 256;
+    static constexpr int CONSUMERS = 512;
     static constexpr int THREADS = CONSUMERS + 32;
     static constexpr int SMEM_BYTES =
         (NS + (T - 1) * NR) * SLOT_FLOATS * 4 + 128 + 2 * NS * 8;
@@ -48,7 +48,7 @@ __device__ __forceinline__ float4 tb_ld4(const float *p) {
 }
 
 __device__ __forceinline__ void consumer_barrier() {
-    asm volatile("bar.sync 1, 256;" ::: "memory");
+    asm volatile("bar.sync 1, 512;" ::: "memory");
 }
 
 }  // namespace st
@@ -62,12 +62,95 @@ __device__ __forceinline__ bool consumer_barrier_and(bool ok) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.u32 p, %1, 0;\n\t"
-        "bar.red.and.pred p, 1, 256, p;\n\t"
+        "bar.red.and.pred p, 1, 512, p;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(r)
         : "r"((uint32_t)ok)
         : "memory");
     return r != 0;
+}
+
+// One level's plane: units of 4 cells (one float4 chunk of one row).  LAST:
+// the output level (chunks of the output tile only, stored to global memory);
+// otherwise every chunk of the rows [r0, r1), stored to the level's ring slot
+// (border cells keep the centre value).  The unit decomposition is
+// compile-time (NC chunks per row), so no runtime division.
+template <int R, int T, int TX, int TY, bool LAST>
+__device__ __forceinline__ void tb_level(const float *cp, const float *const *zp, float *outp,
+                                         float *__restrict__ dst, const Geom &g, int x0, int y0,
+                                         int gz, int r0, int r1, bool border_plane) {
+    using S = TbShape<R, T, TX, TY>;
+    constexpr int C = 6 * R;
+    constexpr int NCU = LAST ? TX / 4 : S::NC;
+    constexpr int C0 = LAST ? S::HX / 4 : 0;
+    const int units = (r1 - r0) * NCU;
+    const int tid = threadIdx.x;
+    if (border_plane) {  // whole plane outside the update region: copy
+        for (int u = tid; u < units; u += S::CONSUMERS) {
+            const int off = (r0 + u / NCU) * S::PW + 4 * (C0 + u % NCU);
+            *reinterpret_cast<float4 *>(outp + off) = tb_ld4(cp + off);
+        }
+        return;
+    }
+#pragma unroll 2
+    for (int u = tid; u < units; u += S::CONSUMERS) {
+        const int row = r0 + u / NCU, c = C0 + u % NCU;
+        const int off = row * S::PW + 4 * c;
+        const float4 left = tb_ld4(cp + off - (c > 0 ? 4 : 0));
+        const float4 mid = tb_ld4(cp + off);
+        const float4 right = tb_ld4(cp + off + (c < S::NC - 1 ? 4 : 0));
+        const float w[12] = {left.x, left.y, left.z, left.w, mid.x, mid.y, mid.z,
+                             mid.w, right.x, right.y, right.z, right.w};
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int o = -R; o <= R; ++o) {
+            if (!o) continue;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[e] += w[4 + e + o];
+        }
+#pragma unroll
+        for (int o = -R; o <= R; ++o) {
+            if (!o) continue;
+            const float4 v = tb_ld4(cp + off + o * S::PW);
+            acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
+        }
+#pragma unroll
+        for (int o = -R; o <= R; ++o) {
+            if (!o) continue;
+            const float4 v = tb_ld4(zp[o + R] + off);
+            acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
+        }
+        // +0 sums are exact on the fast path (a sum never yields -0)
+        float a4[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) a4[e] = acc[e] == 0.0f ? 1.0f : fabsf(acc[e]);
+        const float lo4 = fminf(fminf(a4[0], a4[1]), fminf(a4[2], a4[3]));
+        const float hi4 = fmaxf(fmaxf(a4[0], a4[1]), fmaxf(a4[2], a4[3]));
+        if (__all_sync(__activemask(), lo4 >= 0x1p-100f && hi4 <= 0x1p+120f)) {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[e] = div_fast<C>(acc[e]);
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[e] = acc[e] / (float)C;
+        }
+        const int gx0 = x0 - S::HX + 4 * c, gy = y0 - S::HY + row;
+        const bool yin = in_range(gy, g.ny, R);
+        if (!LAST) {
+            float o4[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) o4[e] = (yin && in_range(gx0 + e, g.nx, R)) ? acc[e] : w[4 + e];
+            *reinterpret_cast<float4 *>(outp + off) = make_float4(o4[0], o4[1], o4[2], o4[3]);
+        } else if (yin && gx0 < g.nx) {
+            float *d = dst + (long long)gz * g.sz + (long long)gy * g.sy + gx0;
+            if (gx0 >= R && gx0 + 3 < g.nx - R) {
+                stg4(d, acc[0], acc[1], acc[2], acc[3]);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (in_range(gx0 + e, g.nx, R)) d[e] = acc[e];
+            }
+        }
+    }
 }
 
 template <int R, int T, int TX, int TY>
@@ -153,84 +236,15 @@ __global__ void __launch_bounds__(TbShape<R, T, TX, TY>::THREADS, 1)
                     };
                     const int r0 = lvl * R, r1 = S::PH - lvl * R;
                     const bool border_plane = q < R || q >= g.nz - R;
-                    const int c0 = lvl == T ? S::HX / 4 : 0;
-                    const int nc = lvl == T ? TX / 4 : S::NC;
-                    const int units = (r1 - r0) * nc;
                     const float *cp = prev(q);
                     float *outp = lvl < T ? planeL(lvl, q) : nullptr;
-                    if (border_plane) {
-                        if (lvl < T)
-                            for (int u = tid; u < units; u += S::CONSUMERS) {
-                                const int row = r0 + u / nc, c = c0 + u % nc;
-                                *reinterpret_cast<float4 *>(outp + row * S::PW + 4 * c) =
-                                    tb_ld4(cp + row * S::PW + 4 * c);
-                            }
-                    } else {
-                        const float *zp[2 * R + 1];
+                    const float *zp[2 * R + 1];
 #pragma unroll
-                        for (int o = -R; o <= R; ++o) zp[o + R] = o ? prev(q + o) : cp;
-                        const int gz = q;
-#pragma unroll 2
-                        for (int u = tid; u < units; u += S::CONSUMERS) {
-                            const int row = r0 + u / nc, c = c0 + u % nc;
-                            const int off = row * S::PW + 4 * c;
-                            const float4 left = tb_ld4(cp + row * S::PW + 4 * max(c - 1, 0));
-                            const float4 mid = tb_ld4(cp + off);
-                            const float4 right = tb_ld4(cp + row * S::PW + 4 * min(c + 1, S::NC - 1));
-                            const float w[12] = {left.x, left.y, left.z, left.w, mid.x, mid.y, mid.z,
-                                                 mid.w, right.x, right.y, right.z, right.w};
-                            float acc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-                            for (int o = -R; o <= R; ++o) {
-                                if (!o) continue;
-#pragma unroll
-                                for (int e = 0; e < 4; ++e) acc[e] += w[4 + e + o];
-                            }
-#pragma unroll
-                            for (int o = -R; o <= R; ++o) {
-                                if (!o) continue;
-                                const float4 v = tb_ld4(cp + off + o * S::PW);
-                                acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
-                            }
-#pragma unroll
-                            for (int o = -R; o <= R; ++o) {
-                                if (!o) continue;
-                                const float4 v = tb_ld4(zp[o + R] + off);
-                                acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
-                            }
-                            // +0 sums are exact on the fast path (a sum never yields -0)
-                            float a4[4];
-#pragma unroll
-                            for (int e = 0; e < 4; ++e) a4[e] = acc[e] == 0.0f ? 1.0f : fabsf(acc[e]);
-                            const float lo4 = fminf(fminf(a4[0], a4[1]), fminf(a4[2], a4[3]));
-                            const float hi4 = fmaxf(fmaxf(fabsf(acc[0]), fabsf(acc[1])), fmaxf(fabsf(acc[2]), fabsf(acc[3])));
-                            if (__all_sync(__activemask(), lo4 >= 0x1p-100f && hi4 <= 0x1p+120f)) {
-#pragma unroll
-                                for (int e = 0; e < 4; ++e) acc[e] = div_fast<C>(acc[e]);
-                            } else {
-#pragma unroll
-                                for (int e = 0; e < 4; ++e) acc[e] = acc[e] / (float)C;
-                            }
-                            const int gx0 = x0 - S::HX + 4 * c, gy = y0 - S::HY + row;
-                            const bool yin = in_range(gy, g.ny, R);
-                            if (lvl < T) {
-                                float o4[4];
-#pragma unroll
-                                for (int e = 0; e < 4; ++e)
-                                    o4[e] = (yin && in_range(gx0 + e, g.nx, R)) ? acc[e] : w[4 + e];
-                                *reinterpret_cast<float4 *>(outp + off) = make_float4(o4[0], o4[1], o4[2], o4[3]);
-                            } else if (yin && gx0 < g.nx) {
-                                float *d = dst + (long long)gz * g.sz + (long long)gy * g.sy + gx0;
-                                if (gx0 >= R && gx0 + 3 < g.nx - R) {
-                                    stg4(d, acc[0], acc[1], acc[2], acc[3]);
-                                } else {
-#pragma unroll
-                                    for (int e = 0; e < 4; ++e)
-                                        if (in_range(gx0 + e, g.nx, R)) d[e] = acc[e];
-                                }
-                            }
-                        }
-                    }
+                    for (int o = -R; o <= R; ++o) zp[o + R] = (o && !border_plane) ? prev(q + o) : cp;
+                    if (lvl < T)
+                        tb_level<R, T, TX, TY, false>(cp, zp, outp, dst, g, x0, y0, q, r0, r1, border_plane);
+                    else if (!border_plane)
+                        tb_level<R, T, TX, TY, true>(cp, zp, outp, dst, g, x0, y0, q, r0, r1, false);
                 }
                 consumer_barrier();
                 // Level 1 no longer needs level-0 plane p - 2R: hand its slot back.
