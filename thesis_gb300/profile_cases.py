@@ -21,6 +21,12 @@ def main(case):
         a, b = u.clone(), u.clone()
         for _ in range(4):
             S.sweep(a, b, R, 2, J, "smem_register")
+    elif case in ("tb_r1_t2", "tb_r1_t4"):
+        T = 2 if case.endswith("t2") else 4
+        u = S.init_uniform((320, 320, 320), 1)
+        a, b = u.clone(), u.clone()
+        for _ in range(4):
+            S.sweep(a, b, 1, T, J, "coop", temporal=T)
     elif case == "base_r1":
         u = S.init_uniform((320, 320, 320), 1)
         a, b = u.clone(), u.clone()
