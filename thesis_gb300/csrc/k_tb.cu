@@ -70,85 +70,106 @@ __device__ __forceinline__ bool consumer_barrier_and(bool ok) {
     return r != 0;
 }
 
-// One level's plane: units of 4 cells (one float4 chunk of one row).  LAST:
-// the output level (chunks of the output tile only, stored to global memory);
-// otherwise every chunk of the rows [r0, r1), stored to the level's ring slot
-// (border cells keep the centre value).  The unit decomposition is
-// compile-time (NC chunks per row), so no runtime division.
+// One unit: 4 cells (one float4 chunk c of one row) of a level's plane.
+// xmask: bit e set if cell e of the chunk lies in the update range along x.
+template <int R, int T, int TX, int TY, bool LAST>
+__device__ __forceinline__ void tb_unit(const float *cp, const float *const *zp, float *outp,
+                                        float *drow, int row, int c, unsigned xmask, bool yin,
+                                        bool xin4) {
+    using S = TbShape<R, T, TX, TY>;
+    constexpr int C = 6 * R;
+    const int off = row * S::PW + 4 * c;
+    const float4 left = tb_ld4(cp + off - (c > 0 ? 4 : 0));
+    const float4 mid = tb_ld4(cp + off);
+    const float4 right = tb_ld4(cp + off + (c < S::NC - 1 ? 4 : 0));
+    const float w[12] = {left.x, left.y, left.z, left.w, mid.x, mid.y, mid.z,
+                         mid.w, right.x, right.y, right.z, right.w};
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int o = -R; o <= R; ++o) {
+        if (!o) continue;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[e] += w[4 + e + o];
+    }
+#pragma unroll
+    for (int o = -R; o <= R; ++o) {
+        if (!o) continue;
+        const float4 v = tb_ld4(cp + off + o * S::PW);
+        acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
+    }
+#pragma unroll
+    for (int o = -R; o <= R; ++o) {
+        if (!o) continue;
+        const float4 v = tb_ld4(zp[o + R] + off);
+        acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
+    }
+    // +0 sums are exact on the fast path (a sum never yields -0)
+    float a4[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) a4[e] = acc[e] == 0.0f ? 1.0f : fabsf(acc[e]);
+    const float lo4 = fminf(fminf(a4[0], a4[1]), fminf(a4[2], a4[3]));
+    const float hi4 = fmaxf(fmaxf(a4[0], a4[1]), fmaxf(a4[2], a4[3]));
+    if (__all_sync(__activemask(), lo4 >= 0x1p-100f && hi4 <= 0x1p+120f)) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[e] = div_fast<C>(acc[e]);
+    } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[e] = acc[e] / (float)C;
+    }
+    if (!LAST) {
+        float o4[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) o4[e] = (yin && ((xmask >> e) & 1)) ? acc[e] : w[4 + e];
+        *reinterpret_cast<float4 *>(outp + off) = make_float4(o4[0], o4[1], o4[2], o4[3]);
+    } else if (yin) {
+        if (xin4) {
+            stg4(drow, acc[0], acc[1], acc[2], acc[3]);
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if ((xmask >> e) & 1) drow[e] = acc[e];
+        }
+    }
+}
+
+// One level's plane.  Warp w owns rows r0 + w, r0 + w + 16, ...; lane l owns
+// chunk 1 + l (the 32 chunks of the output tile's columns).  Levels below T
+// also need the two edge chunks of each row (their halo cells); those units
+// go to the last warps, which own fewer rows.  Border cells (outside the
+// update region) keep the centre value; the whole-plane border case copies.
 template <int R, int T, int TX, int TY, bool LAST>
 __device__ __forceinline__ void tb_level(const float *cp, const float *const *zp, float *outp,
                                          float *__restrict__ dst, const Geom &g, int x0, int y0,
-                                         int gz, int r0, int r1, bool border_plane) {
+                                         int gz, int r0, int r1, bool border_plane,
+                                         unsigned lane_xmask, unsigned edge_xmask0,
+                                         unsigned edge_xmask1) {
     using S = TbShape<R, T, TX, TY>;
-    constexpr int C = 6 * R;
-    constexpr int NCU = LAST ? TX / 4 : S::NC;
-    constexpr int C0 = LAST ? S::HX / 4 : 0;
-    const int units = (r1 - r0) * NCU;
-    const int tid = threadIdx.x;
-    if (border_plane) {  // whole plane outside the update region: copy
-        for (int u = tid; u < units; u += S::CONSUMERS) {
-            const int off = (r0 + u / NCU) * S::PW + 4 * (C0 + u % NCU);
+    static_assert(S::NC == TX / 4 + 2 && S::HX == 4, "one edge chunk per side");
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int c = 1 + lane;
+    if (border_plane) {  // whole plane outside the update region: copy (levels < T only)
+        for (int u = tid; u < (r1 - r0) * S::NC; u += S::CONSUMERS) {
+            const int off = (r0 + u / S::NC) * S::PW + 4 * (u % S::NC);
             *reinterpret_cast<float4 *>(outp + off) = tb_ld4(cp + off);
         }
         return;
     }
-#pragma unroll 2
-    for (int u = tid; u < units; u += S::CONSUMERS) {
-        const int row = r0 + u / NCU, c = C0 + u % NCU;
-        const int off = row * S::PW + 4 * c;
-        const float4 left = tb_ld4(cp + off - (c > 0 ? 4 : 0));
-        const float4 mid = tb_ld4(cp + off);
-        const float4 right = tb_ld4(cp + off + (c < S::NC - 1 ? 4 : 0));
-        const float w[12] = {left.x, left.y, left.z, left.w, mid.x, mid.y, mid.z,
-                             mid.w, right.x, right.y, right.z, right.w};
-        float acc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int o = -R; o <= R; ++o) {
-            if (!o) continue;
-#pragma unroll
-            for (int e = 0; e < 4; ++e) acc[e] += w[4 + e + o];
-        }
-#pragma unroll
-        for (int o = -R; o <= R; ++o) {
-            if (!o) continue;
-            const float4 v = tb_ld4(cp + off + o * S::PW);
-            acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
-        }
-#pragma unroll
-        for (int o = -R; o <= R; ++o) {
-            if (!o) continue;
-            const float4 v = tb_ld4(zp[o + R] + off);
-            acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
-        }
-        // +0 sums are exact on the fast path (a sum never yields -0)
-        float a4[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) a4[e] = acc[e] == 0.0f ? 1.0f : fabsf(acc[e]);
-        const float lo4 = fminf(fminf(a4[0], a4[1]), fminf(a4[2], a4[3]));
-        const float hi4 = fmaxf(fmaxf(a4[0], a4[1]), fmaxf(a4[2], a4[3]));
-        if (__all_sync(__activemask(), lo4 >= 0x1p-100f && hi4 <= 0x1p+120f)) {
-#pragma unroll
-            for (int e = 0; e < 4; ++e) acc[e] = div_fast<C>(acc[e]);
-        } else {
-#pragma unroll
-            for (int e = 0; e < 4; ++e) acc[e] = acc[e] / (float)C;
-        }
-        const int gx0 = x0 - S::HX + 4 * c, gy = y0 - S::HY + row;
+    const int gx0 = x0 - S::HX + 4 * c;
+    const bool xin4 = lane_xmask == 0xFu;
+    for (int row = r0 + warp; row < r1; row += S::CONSUMERS / 32) {
+        const int gy = y0 - S::HY + row;
         const bool yin = in_range(gy, g.ny, R);
-        if (!LAST) {
-            float o4[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) o4[e] = (yin && in_range(gx0 + e, g.nx, R)) ? acc[e] : w[4 + e];
-            *reinterpret_cast<float4 *>(outp + off) = make_float4(o4[0], o4[1], o4[2], o4[3]);
-        } else if (yin && gx0 < g.nx) {
-            float *d = dst + (long long)gz * g.sz + (long long)gy * g.sy + gx0;
-            if (gx0 >= R && gx0 + 3 < g.nx - R) {
-                stg4(d, acc[0], acc[1], acc[2], acc[3]);
-            } else {
-#pragma unroll
-                for (int e = 0; e < 4; ++e)
-                    if (in_range(gx0 + e, g.nx, R)) d[e] = acc[e];
-            }
+        float *drow = LAST ? dst + (long long)gz * g.sz + (long long)gy * g.sy + gx0 : nullptr;
+        tb_unit<R, T, TX, TY, LAST>(cp, zp, outp, drow, row, c, lane_xmask, yin, xin4);
+    }
+    if (!LAST) {
+        const int et = S::CONSUMERS - 1 - tid;  // edge units on the last threads
+        if (et < 2 * (r1 - r0)) {
+            const int row = r0 + (et >> 1), side = et & 1;
+            const int gy = y0 - S::HY + row;
+            tb_unit<R, T, TX, TY, false>(cp, zp, outp, nullptr, row, side ? S::NC - 1 : 0,
+                                         side ? edge_xmask1 : edge_xmask0, in_range(gy, g.ny, R),
+                                         false);
         }
     }
 }
@@ -213,6 +234,16 @@ __global__ void __launch_bounds__(TbShape<R, T, TX, TY>::THREADS, 1)
         i = (long long)t * zin + (zb - R);
         const int x0 = (t % tiles_x) * TX, y0 = (t / tiles_x) * TY;
         const int p0 = max(0, za - T * R), h0 = min(g.nz, zb + T * R);
+        auto xmask_of = [&](int chunk) {
+            unsigned m = 0;
+            const int gx = x0 - S::HX + 4 * chunk;
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (in_range(gx + e, g.nx, R)) m |= 1u << e;
+            return m;
+        };
+        const unsigned lane_xmask = xmask_of(1 + (tid & 31));
+        const unsigned edge_xmask0 = xmask_of(0), edge_xmask1 = xmask_of(S::NC - 1);
         auto plane0 = [&](int z) -> float * {
             return ring0 + ((qb + (uint32_t)(z - p0)) % S::NS) * S::SLOT_FLOATS;
         };
@@ -242,9 +273,12 @@ __global__ void __launch_bounds__(TbShape<R, T, TX, TY>::THREADS, 1)
 #pragma unroll
                     for (int o = -R; o <= R; ++o) zp[o + R] = (o && !border_plane) ? prev(q + o) : cp;
                     if (lvl < T)
-                        tb_level<R, T, TX, TY, false>(cp, zp, outp, dst, g, x0, y0, q, r0, r1, border_plane);
+                        tb_level<R, T, TX, TY, false>(cp, zp, outp, dst, g, x0, y0, q, r0, r1,
+                                                      border_plane, lane_xmask, edge_xmask0,
+                                                      edge_xmask1);
                     else if (!border_plane)
-                        tb_level<R, T, TX, TY, true>(cp, zp, outp, dst, g, x0, y0, q, r0, r1, false);
+                        tb_level<R, T, TX, TY, true>(cp, zp, outp, dst, g, x0, y0, q, r0, r1,
+                                                     false, lane_xmask, edge_xmask0, edge_xmask1);
                 }
                 consumer_barrier();
                 // Level 1 no longer needs level-0 plane p - 2R: hand its slot back.
