@@ -268,13 +268,14 @@ StreamKernel sk() {
             S::SMEM_BYTES};
 }
 
-// shape: 0 = default (128 x 16), 1 = tall (64 x 32)
+// shape: 0 = default (128 x 16, 2 rows per thread), 1 = tall (64 x 32),
+// 2 = one row per thread (more warps, fewer registers each)
 StreamKernel pick(int r, int shape) {
     switch (r) {
-        case 1: return shape == 1 ? sk<1, 64, 32, 2, 8>() : sk<1, 128, 16, 2, 8>();
-        case 2: return shape == 1 ? sk<2, 64, 32, 2, 8>() : sk<2, 128, 16, 2, 8>();
+        case 1: return shape == 2 ? sk<1, 128, 16, 1, 8>() : shape == 1 ? sk<1, 64, 32, 2, 8>() : sk<1, 128, 16, 2, 8>();
+        case 2: return shape == 2 ? sk<2, 128, 16, 1, 8>() : shape == 1 ? sk<2, 64, 32, 2, 8>() : sk<2, 128, 16, 2, 8>();
         case 3: return shape == 1 ? sk<3, 64, 32, 2, 8>() : sk<3, 128, 16, 2, 8>();
-        case 4: return shape == 1 ? sk<4, 64, 32, 2, 8>() : sk<4, 128, 16, 2, 8>();
+        case 4: return shape == 2 ? sk<4, 128, 8, 1, 8>() : shape == 1 ? sk<4, 64, 32, 2, 8>() : sk<4, 128, 16, 2, 8>();
         default: return {nullptr, 0, 0, 0, 0};
     }
 }
@@ -288,7 +289,7 @@ bool stream3d_supported(const Geom &g) {
 int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int tile_y,
                  cudaStream_t s, float **res) {
     const int R = g.radius;
-    const int shape = (tile_x && tile_x < 128) || tile_y > 16 ? 1 : 0;
+    const int shape = tile_y == 1 ? 2 : ((tile_x && tile_x < 128) || tile_y > 16 ? 1 : 0);
     StreamKernel k = pick(R, shape);
     if (!k.fn) return fail(STENCIL_EUNSUPPORTED, "stream kernel has no radius-%d instance", R);
     if (g.nx % 4) return fail(STENCIL_EUNSUPPORTED, "stream kernel needs nx %% 4 == 0");
