@@ -118,6 +118,84 @@ __device__ __forceinline__ void sweep_slab(const float *src, float *dst, long lo
     }
 }
 
+// 2-D slab sweep with a fixed thread -> (chunk, row block) map: lane group
+// g of the CTA owns a contiguous block of rows, thread c of the group owns
+// float4 chunk c of every row in it.  The chunk's column of the rows j-R ..
+// j+R rides in a register queue down the block (one new 16-byte load per
+// row); only the x-neighbour chunks are loaded per row.  No index division in
+// the loop.  Requires nx / 4 <= blockDim.x.
+template <int R>
+__device__ __forceinline__ void sweep_rows2d(const float *src, float *dst, long long base,
+                                             int s_begin, int s_end, const ClusterJob &j) {
+    constexpr int C = 4 * R;
+    constexpr int RA = (R + 3) & ~3;
+    const int nx = j.nx, ny = j.ny, chunks = nx >> 2;
+    const int G = blockDim.x / chunks;
+    const int c = threadIdx.x % chunks, grp = threadIdx.x / chunks;
+    const int rb = max(s_begin, R), re = min(s_end, ny - R);
+    if (grp >= G || rb >= re) return;
+    const int per = (re - rb + G - 1) / G;
+    const int j0 = rb + grp * per, j1 = min(re, j0 + per);
+    if (j0 >= j1) return;
+    const int x0 = 4 * c;
+    unsigned mask = 0;
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+        if (x0 + e >= R && x0 + e < nx - R) mask |= 1u << e;
+    if (!mask) return;
+    const float *col = src + (long long)(-base) * nx + x0;  // row j of this chunk at col + j*nx
+    float *dcol = dst + (long long)(-base) * nx + x0;
+    float4 q[2 * R + 1];  // rows j-R .. j+R of this chunk
+#pragma unroll
+    for (int k = 0; k < 2 * R; ++k) q[k] = ld4(col + (long long)(j0 - R + k) * nx);
+#pragma unroll 2
+    for (int jj = j0; jj < j1; ++jj) {
+        q[2 * R] = ld4(col + (long long)(jj + R) * nx);
+        const float *row = col + (long long)jj * nx;
+        float w[4 + 2 * RA];
+#pragma unroll
+        for (int h = 0; h < RA / 4; ++h) {
+            float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+            if (c - RA / 4 + h >= 0) a = ld4(row - RA + 4 * h);
+            if (c + 1 + h < chunks) b = ld4(row + 4 + 4 * h);
+            w[4 * h] = a.x; w[4 * h + 1] = a.y; w[4 * h + 2] = a.z; w[4 * h + 3] = a.w;
+            w[RA + 4 + 4 * h] = b.x; w[RA + 5 + 4 * h] = b.y;
+            w[RA + 6 + 4 * h] = b.z; w[RA + 7 + 4 * h] = b.w;
+        }
+        const float4 m = q[R];
+        w[RA] = m.x; w[RA + 1] = m.y; w[RA + 2] = m.z; w[RA + 3] = m.w;
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int o = -R; o <= R; ++o) {
+            if (!o) continue;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[e] += w[RA + e + o];
+        }
+#pragma unroll
+        for (int o = -R; o <= R; ++o) {
+            if (!o) continue;
+            const float4 v = q[R + o];
+            acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
+        }
+        float out[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            out[e] = div_coeff<C>(acc[e]);
+            if (j.legacy) out[e] -= w[RA + e];
+        }
+        float *d = dcol + (long long)jj * nx;
+        if (mask == 0xFu) {
+            *reinterpret_cast<float4 *>(d) = make_float4(out[0], out[1], out[2], out[3]);
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if ((mask >> e) & 1) d[e] = out[e];
+        }
+#pragma unroll
+        for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];
+    }
+}
+
 // Copies slices [s_begin, s_end) between a global grid and a local slab.
 __device__ __forceinline__ void copy_slices(float *to, const float *from, long long count4) {
     for (long long i = threadIdx.x; i < count4; i += blockDim.x)
@@ -144,7 +222,10 @@ __device__ void run_job(const ClusterJob &j, float *smem, uint32_t rank, uint32_
         const uint32_t my0 = smem_u32(buf[0]);
         int cur = 0;
         for (int it = 0; it < j.iters; ++it) {
-            sweep_slab<D, R>(buf[cur], buf[cur ^ 1], s0 - R, s0, s1, j);
+            if (D == 2 && (j.nx >> 2) <= (int)blockDim.x)
+                sweep_rows2d<R>(buf[cur], buf[cur ^ 1], s0 - R, s0, s1, j);
+            else
+                sweep_slab<D, R>(buf[cur], buf[cur ^ 1], s0 - R, s0, s1, j);
             __syncthreads();
             // Push the first / last R owned slices into the neighbours' halos.
             const long long n4 = (long long)R * slice_len / 4;

@@ -289,7 +289,10 @@ bool stream3d_supported(const Geom &g) {
 int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int tile_y,
                  cudaStream_t s, float **res) {
     const int R = g.radius;
-    const int shape = tile_y == 1 ? 2 : ((tile_x && tile_x < 128) || tile_y > 16 ? 1 : 0);
+    // one row per thread is the default for R = 2 (measured fastest at 512^3)
+    const int shape = tile_y == 1 || (R == 2 && !tile_x && !tile_y)
+                          ? 2
+                          : ((tile_x && tile_x < 128) || tile_y > 16 ? 1 : 0);
     StreamKernel k = pick(R, shape);
     if (!k.fn) return fail(STENCIL_EUNSUPPORTED, "stream kernel has no radius-%d instance", R);
     if (g.nx % 4) return fail(STENCIL_EUNSUPPORTED, "stream kernel needs nx %% 4 == 0");
