@@ -38,6 +38,8 @@ struct ClusterJob {
     float *a, *b;       // caller buffers (a = initial state)
     int dims, nx, ny, nz;
     int radius, iters, legacy, resident;
+    int tblock;         // resident mode: sweeps between halo exchanges (>= 1)
+    int pad;
 };
 
 constexpr int kClusterThreads = 512;
@@ -209,45 +211,61 @@ __device__ void run_job(const ClusterJob &j, float *smem, uint32_t rank, uint32_
     const int H = (S + csize - 1) / csize;
     const int s0 = min((int)rank * H, S), s1 = min(s0 + H, S);
     if (j.resident) {
-        // Slab with halo: local slice k <-> global slice s0 - R + k.
-        const long long slab = (long long)(H + 2 * R) * slice_len;
+        // Slab with a halo of HT = tblock * R slices per side: local slice k
+        // <-> global slice s0 - HT + k.  Between halo exchanges the CTA runs
+        // tblock sweeps; sweep k of a block also updates the (tblock - k) * R
+        // halo slices next to its own slab (a trapezoid), with arithmetic
+        // identical to the owner's, so one exchange serves tblock sweeps.
+        const int TB = j.tblock, HT = TB * R;
+        const long long slab = (long long)(H + 2 * HT) * slice_len;
         float *buf[2] = {smem, smem + slab};
-        const int l0 = max(s0 - R, 0), l1 = min(s1 + R, S);
+        const int l0 = max(s0 - HT, 0), l1 = min(s1 + HT, S);
         if (l0 < l1) {
-            const long long off = (long long)(l0 - (s0 - R)) * slice_len;
+            const long long off = (long long)(l0 - (s0 - HT)) * slice_len;
             copy_slices(buf[0] + off, j.a + (long long)l0 * slice_len, (l1 - l0) * slice_len / 4);
             copy_slices(buf[1] + off, j.b + (long long)l0 * slice_len, (l1 - l0) * slice_len / 4);
         }
         cluster_sync();
         const uint32_t my0 = smem_u32(buf[0]);
         int cur = 0;
-        for (int it = 0; it < j.iters; ++it) {
-            if (D == 2 && (j.nx >> 2) <= (int)blockDim.x)
-                sweep_rows2d<R>(buf[cur], buf[cur ^ 1], s0 - R, s0, s1, j);
-            else
-                sweep_slab<D, R>(buf[cur], buf[cur ^ 1], s0 - R, s0, s1, j);
-            __syncthreads();
-            // Push the first / last R owned slices into the neighbours' halos.
-            const long long n4 = (long long)R * slice_len / 4;
-            const uint32_t dst_base = my0 + (uint32_t)((cur ^ 1) * slab * 4);
+        for (int it = 0; it < j.iters;) {
+            const int kk = min(TB, j.iters - it);
+            for (int k = 1; k <= kk; ++k) {
+                const int ext = (kk - k) * R;
+                const int a = max(s0 - ext, 0), b = min(s1 + ext, S);
+                if (s1 > s0) {
+                    if (D == 2 && (j.nx >> 2) <= (int)blockDim.x)
+                        sweep_rows2d<R>(buf[cur], buf[cur ^ 1], s0 - HT, a, b, j);
+                    else
+                        sweep_slab<D, R>(buf[cur], buf[cur ^ 1], s0 - HT, a, b, j);
+                }
+                __syncthreads();
+                cur ^= 1;
+            }
+            it += kk;
+            if (it >= j.iters) break;
+            // Every CTA has finished reading its halo; refresh the halos of
+            // buf[cur] with the neighbours' newest own slices.
+            if (TB > 1) cluster_sync();
+            const long long n4 = (long long)HT * slice_len / 4;
+            const uint32_t dst_base = my0 + (uint32_t)(cur * slab * 4);
             if (rank > 0 && s1 > s0) {
-                // my slices s0..s0+R-1 -> rank-1's local slices H+R .. H+2R-1
-                const float4 *from = reinterpret_cast<const float4 *>(buf[cur ^ 1] + (long long)R * slice_len);
-                const uint32_t to = mapa_shared(dst_base + (uint32_t)((long long)(H + R) * slice_len * 4), rank - 1);
+                // my slices s0 .. s0+HT-1 -> rank-1's local slices H+HT .. H+2HT-1
+                const float4 *from = reinterpret_cast<const float4 *>(buf[cur] + (long long)HT * slice_len);
+                const uint32_t to = mapa_shared(dst_base + (uint32_t)((long long)(H + HT) * slice_len * 4), rank - 1);
                 for (long long i = threadIdx.x; i < n4; i += blockDim.x) st_cluster_v4(to + (uint32_t)(i * 16), from[i]);
             }
             if (rank + 1 < csize && s1 > s0 && s1 < S) {
-                // my slices s1-R..s1-1 -> rank+1's local slices 0..R-1
-                const float4 *from = reinterpret_cast<const float4 *>(buf[cur ^ 1] + (long long)(s1 - R - (s0 - R)) * slice_len);
+                // my slices s1-HT .. s1-1 -> rank+1's local slices 0 .. HT-1
+                const float4 *from = reinterpret_cast<const float4 *>(buf[cur] + (long long)(s1 - s0) * slice_len);
                 const uint32_t to = mapa_shared(dst_base, rank + 1);
                 for (long long i = threadIdx.x; i < n4; i += blockDim.x) st_cluster_v4(to + (uint32_t)(i * 16), from[i]);
             }
             cluster_sync();
-            cur ^= 1;
         }
         // Both buffers back to the caller's buffers (owned slices only).
         if (s1 > s0) {
-            const long long off = (long long)R * slice_len;
+            const long long off = (long long)HT * slice_len;
             float *ga = (j.iters & 1) ? j.b : j.a;  // holds buf[cur]
             float *gb = (j.iters & 1) ? j.a : j.b;
             copy_slices(ga + (long long)s0 * slice_len, buf[cur] + off, (s1 - s0) * slice_len / 4);
@@ -320,11 +338,11 @@ __global__ void __launch_bounds__(kClusterThreads)
 // ---------------------------------------------------------------------------
 constexpr int kClusterSmemMax = 200 * 1024;
 
-static long long slab_bytes(const ClusterJob &j, int csize) {
+static long long slab_bytes(const ClusterJob &j, int csize, int tblock) {
     const int S = j.dims == 3 ? j.nz : j.ny;
     const long long slice_len = j.dims == 3 ? (long long)j.nx * j.ny : j.nx;
     const int H = (S + csize - 1) / csize;
-    return 2LL * (H + 2 * j.radius) * slice_len * 4;
+    return 2LL * (H + 2 * tblock * j.radius) * slice_len * 4;
 }
 
 bool cluster_job_ok(int dims, int nx, int ny, int nz, int radius) {
@@ -334,12 +352,23 @@ bool cluster_job_ok(int dims, int nx, int ny, int nz, int radius) {
 
 // Resident when the slab fits and every CTA that owns slices owns at least R
 // (so each halo comes from one neighbour).
+// The sweeps between halo exchanges: the largest of 4, 2, 1 whose deeper
+// halo still fits and is owned by a single neighbour.
 static void plan_job(ClusterJob &j, int csize) {
     const int S = j.dims == 3 ? j.nz : j.ny;
     const int H = (S + csize - 1) / csize;
     const int last = S - ((S + H - 1) / H - 1) * H;
-    j.resident = (slab_bytes(j, csize) + 128 <= kClusterSmemMax && H >= j.radius &&
-                  last >= j.radius) ? 1 : 0;
+    j.resident = 0;
+    j.tblock = 1;
+    j.pad = 0;
+    for (int tb : {4, 2, 1}) {
+        const int ht = tb * j.radius;
+        if (slab_bytes(j, csize, tb) + 128 <= kClusterSmemMax && H >= ht && last >= ht) {
+            j.resident = 1;
+            j.tblock = (csize == 1) ? 1 : tb;
+            break;
+        }
+    }
 }
 
 // Function attributes of k_cluster (once per device, outside any capture).
