@@ -20,6 +20,8 @@ int launch_residual(const Geom &g, int dims, const float *u, double *scratch, cu
 bool stream3d_supported(const Geom &g);
 bool tile_supported(const Geom &g, int dims);
 bool tb3d_supported(const Geom &g);
+bool rows3d_supported(const Geom &g);
+int run_rows3d(const Geom &g, float *a, float *b, int iters, cudaStream_t s, float **res);
 
 static thread_local char t_err[512];
 
@@ -294,6 +296,14 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
     if (variant == STENCIL_VARIANT_COOP)
         variant = p->dims == 3 && stream3d_supported(g) ? STENCIL_VARIANT_SMEM_REGISTER
                                                         : STENCIL_VARIANT_BASE;
+    if (variant == STENCIL_VARIANT_SMEM_REGISTER && p->block_x == 0 && p->block_y == 8 &&
+        rows3d_supported(g)) {
+        float *res = nullptr;
+        rc = run_rows3d(g, cur, nxt, p->iterations, s, &res);
+        if (rc) return rc;
+        if (d_result) *d_result = res;
+        return STENCIL_OK;
+    }
     if (variant == STENCIL_VARIANT_SMEM_REGISTER) {
         float *res = nullptr;
         rc = run_stream3d(g, cur, nxt, p->iterations, p->block_x ? 4 * p->block_x : 0,
