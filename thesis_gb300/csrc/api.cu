@@ -21,7 +21,8 @@ bool stream3d_supported(const Geom &g);
 bool tile_supported(const Geom &g, int dims);
 bool tb3d_supported(const Geom &g);
 bool rows3d_supported(const Geom &g);
-int run_rows3d(const Geom &g, float *a, float *b, int iters, cudaStream_t s, float **res);
+int run_rows3d(const Geom &g, float *a, float *b, int iters, int shape, cudaStream_t s,
+               float **res);
 
 static thread_local char t_err[512];
 
@@ -299,7 +300,7 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
     if (variant == STENCIL_VARIANT_SMEM_REGISTER && p->block_x == 0 && p->block_y == 8 &&
         rows3d_supported(g)) {
         float *res = nullptr;
-        rc = run_rows3d(g, cur, nxt, p->iterations, s, &res);
+        rc = run_rows3d(g, cur, nxt, p->iterations, p->block_z, s, &res);
         if (rc) return rc;
         if (d_result) *d_result = res;
         return STENCIL_OK;

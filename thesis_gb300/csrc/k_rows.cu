@@ -230,8 +230,13 @@ RowsKernel rk(int nx) {
             S::threads(nx)};
 }
 
-RowsKernel pick_rows(int r, int nx) {
-    if (r == 1) return rk<1, 8, 2, 8>(nx);
+// shape 0: 8 rows per slab, ring of 8; 1: 4 rows, ring of 16; 2: 16 rows, ring of 4.
+RowsKernel pick_rows(int r, int nx, int shape = 0) {
+    if (r == 1) {
+        if (shape == 1) return rk<1, 4, 1, 16>(nx);
+        if (shape == 2) return rk<1, 16, 4, 4>(nx);
+        return rk<1, 8, 2, 8>(nx);
+    }
     if (r == 2) return rk<2, 8, 2, 8>(nx);
     return {nullptr, 0, 0, 0};
 }
@@ -244,10 +249,13 @@ bool rows3d_supported(const Geom &g) {
     return k.fn && k.smem <= 227 * 1024 && k.threads <= kRowsMaxThreads;
 }
 
-int run_rows3d(const Geom &g, float *a, float *b, int iters, cudaStream_t s, float **res) {
+int run_rows3d(const Geom &g, float *a, float *b, int iters, int shape, cudaStream_t s,
+               float **res) {
     if (!rows3d_supported(g)) return fail(STENCIL_EUNSUPPORTED, "row-slab kernel: nx %% 128, R <= 2, nx small enough");
     const int R = g.radius;
-    RowsKernel k = pick_rows(R, g.nx);
+    RowsKernel k = pick_rows(R, g.nx, shape);
+    if (k.smem > 227 * 1024 || k.threads > kRowsMaxThreads)
+        return fail(STENCIL_EUNSUPPORTED, "row-slab shape %d does not fit nx %d", shape, g.nx);
     ST_CUDA(cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, k.smem));
     int per_sm = 0;
     ST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, k.threads, k.smem));
