@@ -31,7 +31,7 @@ __device__ __forceinline__ float4 rl4(const float *p) { return *reinterpret_cast
 constexpr int kRowsMaxThreads = 544;
 
 template <int R, int TY, int RY, int NS>
-__global__ void __launch_bounds__(kRowsMaxThreads, 1)
+__global__ void __launch_bounds__(128 * (TY / RY) + 32, 1)
     k_rows3d(const float *__restrict__ src, float *__restrict__ dst, Geom g, int zchunk,
              int items) {
     using S = RowsShape<R, TY, RY, NS>;
@@ -230,28 +230,38 @@ RowsKernel rk(int nx) {
             S::threads(nx)};
 }
 
-// shape 0: 8 rows per slab, ring of 8; 1: 4 rows, ring of 16; 2: 16 rows, ring of 4.
+// Slab shapes (rows per CTA, rows per thread, ring slots).  shape 0 is the
+// default per radius (fastest measured at 512^3); 1 and 2 are alternatives
+// for the tuner.  Deep rings (many planes in flight) matter most.
 RowsKernel pick_rows(int r, int nx, int shape = 0) {
-    if (r == 1) {
-        if (shape == 1) return rk<1, 4, 1, 16>(nx);
-        if (shape == 2) return rk<1, 16, 4, 4>(nx);
-        return rk<1, 8, 2, 8>(nx);
+    switch (r) {
+        case 1:
+            if (shape == 1) return rk<1, 8, 2, 8>(nx);
+            if (shape == 2) return rk<1, 16, 4, 4>(nx);
+            return rk<1, 4, 1, 16>(nx);
+        case 2:
+            if (shape == 1) return rk<2, 8, 2, 8>(nx);
+            if (shape == 2) return rk<2, 2, 1, 16>(nx);
+            return rk<2, 4, 1, 8>(nx);
+        case 4:
+            if (shape == 1) return rk<4, 4, 1, 8>(nx);
+            return rk<4, 2, 1, 8>(nx);
+        default:
+            return {nullptr, 0, 0, 0};
     }
-    if (r == 2) return rk<2, 8, 2, 8>(nx);
-    return {nullptr, 0, 0, 0};
 }
 
 }  // namespace
 
 bool rows3d_supported(const Geom &g) {
-    if (g.nx % 128 || g.radius < 1 || g.radius > 2) return false;
+    if (g.nx % 128 || g.radius < 1 || g.radius > 4) return false;
     RowsKernel k = pick_rows(g.radius, g.nx);
     return k.fn && k.smem <= 227 * 1024 && k.threads <= kRowsMaxThreads;
 }
 
 int run_rows3d(const Geom &g, float *a, float *b, int iters, int shape, cudaStream_t s,
                float **res) {
-    if (!rows3d_supported(g)) return fail(STENCIL_EUNSUPPORTED, "row-slab kernel: nx %% 128, R <= 2, nx small enough");
+    if (!rows3d_supported(g)) return fail(STENCIL_EUNSUPPORTED, "row-slab kernel: nx %% 128 == 0, nx <= 512, R in {1, 2, 4}");
     const int R = g.radius;
     RowsKernel k = pick_rows(R, g.nx, shape);
     if (k.smem > 227 * 1024 || k.threads > kRowsMaxThreads)
