@@ -308,7 +308,7 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
     if (variant == STENCIL_VARIANT_SMEM_REGISTER) {
         float *res = nullptr;
         rc = run_stream3d(g, cur, nxt, p->iterations, p->block_x ? 4 * p->block_x : 0,
-                          p->block_y, s, &res);
+                          p->block_y, s, &res, p->block_z);
         if (rc) return rc;
         if (d_result) *d_result = res;
         return STENCIL_OK;

@@ -39,8 +39,9 @@ int launch_tile_sweep(const Geom &g, int dims, const float *src, float *dst, int
 
 // Multi-sweep drivers: run `iters` sweeps ping-ponging between a and b
 // starting from a; *res receives the buffer holding the final state.
+// shape_hint (block_z of the parameters): 0 = by tile fields, 1..3 = a shape.
 int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int tile_y,
-                 cudaStream_t s, float **res);
+                 cudaStream_t s, float **res, int shape_hint = 0);
 int run_tb3d(const Geom &g, float *a, float *b, int iters, int temporal, cudaStream_t s,
              float **res);
 // All sweeps of one grid on one thread-block cluster (k_cluster.cu).

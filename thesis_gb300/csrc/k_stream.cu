@@ -54,7 +54,7 @@ struct StreamShape {
 __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 
 template <int R, int TX, int TY, int RY, int NS>
-__global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <= 1 ? 2 : 1))
+__global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <= 1 && NS <= 8 ? 2 : 1))
     k_stream3d(const __grid_constant__ CUtensorMap src_map, float *__restrict__ dst, Geom g,
                int tiles_x, int tiles_y, int zchunk, int items) {
     using S = StreamShape<R, TX, TY, RY, NS>;
@@ -268,14 +268,15 @@ StreamKernel sk() {
             S::SMEM_BYTES};
 }
 
-// shape: 0 = default (128 x 16, 2 rows per thread), 1 = tall (64 x 32),
-// 2 = one row per thread (more warps, fewer registers each)
+// shape: 0 = 128 x 16, 2 rows per thread; 1 = tall (64 x 32); 2 = one row
+// per thread (more warps, fewer registers each); 3 = a 16-slot ring (more
+// planes in flight, one CTA per SM)
 StreamKernel pick(int r, int shape) {
     switch (r) {
-        case 1: return shape == 2 ? sk<1, 128, 16, 1, 8>() : shape == 1 ? sk<1, 64, 32, 2, 8>() : sk<1, 128, 16, 2, 8>();
-        case 2: return shape == 2 ? sk<2, 128, 16, 1, 8>() : shape == 1 ? sk<2, 64, 32, 2, 8>() : sk<2, 128, 16, 2, 8>();
+        case 1: return shape == 3 ? sk<1, 128, 16, 1, 16>() : shape == 2 ? sk<1, 128, 16, 1, 8>() : shape == 1 ? sk<1, 64, 32, 2, 8>() : sk<1, 128, 16, 2, 8>();
+        case 2: return shape == 3 ? sk<2, 128, 16, 1, 16>() : shape == 2 ? sk<2, 128, 16, 1, 8>() : shape == 1 ? sk<2, 64, 32, 2, 8>() : sk<2, 128, 16, 2, 8>();
         case 3: return shape == 1 ? sk<3, 64, 32, 2, 8>() : sk<3, 128, 16, 2, 8>();
-        case 4: return shape == 2 ? sk<4, 128, 8, 1, 8>() : shape == 1 ? sk<4, 64, 32, 2, 8>() : sk<4, 128, 16, 2, 8>();
+        case 4: return shape == 3 ? sk<4, 128, 16, 2, 16>() : shape == 2 ? sk<4, 128, 8, 1, 8>() : shape == 1 ? sk<4, 64, 32, 2, 8>() : sk<4, 128, 16, 2, 8>();
         default: return {nullptr, 0, 0, 0, 0};
     }
 }
@@ -287,12 +288,13 @@ bool stream3d_supported(const Geom &g) {
 }
 
 int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int tile_y,
-                 cudaStream_t s, float **res) {
+                 cudaStream_t s, float **res, int shape_hint) {
     const int R = g.radius;
     // one row per thread is the default for R = 2 (measured fastest at 512^3)
-    const int shape = tile_y == 1 || (R == 2 && !tile_x && !tile_y)
-                          ? 2
-                          : ((tile_x && tile_x < 128) || tile_y > 16 ? 1 : 0);
+    int shape = tile_y == 1 || (R == 2 && !tile_x && !tile_y)
+                    ? 2
+                    : ((tile_x && tile_x < 128) || tile_y > 16 ? 1 : 0);
+    if (shape_hint >= 1 && shape_hint <= 3) shape = shape_hint;
     StreamKernel k = pick(R, shape);
     if (!k.fn) return fail(STENCIL_EUNSUPPORTED, "stream kernel has no radius-%d instance", R);
     if (g.nx % 4) return fail(STENCIL_EUNSUPPORTED, "stream kernel needs nx %% 4 == 0");
