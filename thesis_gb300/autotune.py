@@ -58,7 +58,10 @@ def variant_space(shape, radius):
         sub["smem_padded"] = {"block": [b for b in block_shapes(dims) if b[0] <= 64]}
         if dims == 3 and radius <= 4:
             top.append({"variant": "smem_register"})
-            sub["smem_register"] = {"block": [(0, 0, 0), (16, 32, 1)]}  # 128 x 16 or 64 x 32 tiles
+            # default shape, 64 x 32 tiles, one row per thread, 16-slot ring,
+            # and (nx % 128 == 0, nx <= 512) the full-width row-slab kernel
+            sub["smem_register"] = {"block": [(0, 0, 0), (16, 32, 1), (0, 1, 0), (0, 0, 3),
+                                              (0, 8, 0), (0, 8, 1)]}
         if radius <= 4:
             top.append({"variant": "cluster"})
             sub["cluster"] = {}

@@ -290,10 +290,11 @@ bool stream3d_supported(const Geom &g) {
 int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int tile_y,
                  cudaStream_t s, float **res, int shape_hint) {
     const int R = g.radius;
-    // one row per thread is the default for R = 2 (measured fastest at 512^3)
-    int shape = tile_y == 1 || (R == 2 && !tile_x && !tile_y)
-                    ? 2
-                    : ((tile_x && tile_x < 128) || tile_y > 16 ? 1 : 0);
+    // Defaults measured fastest at 512^3 on GB300: R = 1 the 16-slot ring
+    // (707 GCell/s vs 615 with 8 slots), R = 2 one row per thread (609 vs 540),
+    // otherwise two rows per thread with an 8-slot ring.
+    int shape = (!tile_x && !tile_y) ? (R == 1 ? 3 : (R == 2 ? 2 : 0))
+                                     : (tile_y == 1 ? 2 : ((tile_x && tile_x < 128) || tile_y > 16 ? 1 : 0));
     if (shape_hint >= 1 && shape_hint <= 3) shape = shape_hint;
     StreamKernel k = pick(R, shape);
     if (!k.fn) return fail(STENCIL_EUNSUPPORTED, "stream kernel has no radius-%d instance", R);
