@@ -111,6 +111,13 @@ STENCIL_API int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float 
  * the start of the upload and the end of the download. */
 STENCIL_API int stencil_run_host(const stencil_params *p, const float *h_in, float *h_out, float *ms);
 
+/* stencil_run_host with two clocks: *ms_total (if non-NULL) as above, and
+ * *ms_sweeps (if non-NULL) the time of the sweeps alone -- the interval the
+ * reference's binary prints as its last stdout line (events around
+ * dispatch_kernels, src/main.cu:58-72 and :89). */
+STENCIL_API int stencil_run_host_timed(const stencil_params *p, const float *h_in, float *h_out,
+                                       float *ms_total, float *ms_sweeps);
+
 /* Device-side initial states (same generators as the CPU oracle). */
 /* include/stencil_initializer.h:6-52: outermost layer 1.0f, everything else 0. */
 STENCIL_API int stencil_init_reference(const stencil_params *p, float *d_u, stencil_stream_t stream);
@@ -221,6 +228,12 @@ STENCIL_API int stencil_residual_noalloc(const stencil_params *p, const float *d
 STENCIL_API const char *stencil_strerror(int status);
 /* Text of the last failure on the calling thread (empty if none). */
 STENCIL_API const char *stencil_last_error(void);
+/* What this thread's last stencil_dispatch_ex (or stencil_run_host*) ran:
+ * the engine ("stream3d", "stream3d-persistent", "rows3d", "tb3d", "cluster",
+ * "base", "tile"; the first one when a dispatch uses two) and how many kernel
+ * launches it made (iterations for one launch per sweep, 1 for the
+ * persistent engines).  For diagnostics and launch accounting. */
+STENCIL_API int stencil_last_dispatch(const char **engine, long long *kernel_launches);
 /* Reads and clears the device-side status word that bounded waits set when
  * they give up (0 = no fault).  Synchronises the device. */
 STENCIL_API int stencil_device_status(int *status);
@@ -253,6 +266,18 @@ STENCIL_API int stencil_tuning_clear(void);
 STENCIL_API int stencil_release(void);
 
 /* Library version and the compute capability it was built for (103). */
+/* The reference's HEURISTIC block shape (set_max_occupancy_block_dimensions,
+ * src/stencil_dispatch.cu:89-101) for a block of `threads` threads (the
+ * reference takes it from cudaOccupancyMaxPotentialBlockSizeVariableSMem,
+ * :143): 3-D: b0 = BLOCK_X (p->block_x), halved while a padded smem block of
+ * b0*R*R cells exceeds the threads; b1 = min(max(2, R), 8); b2 =
+ * threads/(b0*b1); the three sorted in descending order.  2-D: (BLOCK_X,
+ * threads/BLOCK_X, 1).  A pure function: with block = 0 the library uses its
+ * own per-kernel default (or the tuning table) instead; callers that want the
+ * reference's shape pass this result as p->block_*. */
+STENCIL_API int stencil_heuristic_block(const stencil_params *p, int threads, int *bx, int *by,
+                                        int *bz);
+
 STENCIL_API int stencil_version(int *abi_version, int *sm);
 
 #ifdef __cplusplus

@@ -40,6 +40,10 @@ typedef struct unet_act {
  * b: FP32 [y->c] or NULL; relu: 0/1.  x->c multiple of 32, y->c of 32. */
 UNET_API int unet_conv3x3_fwd(const unet_act *x, const void *w, const float *b,
                               const unet_act *y, int relu, stencil_stream_t stream);
+/* The same with the taps `dilation` cells apart (zero padding = dilation):
+ * y[p] = act(b + sum_tap w[tap] x[p + dilation * (ky-1, kx-1)]). */
+UNET_API int unet_conv3x3_fwd_dil(const unet_act *x, const void *w, const float *b,
+                                  const unet_act *y, int relu, int dilation, stencil_stream_t stream);
 /* wt[ci][ky][kx][co] = w[co][2-ky][2-kx][ci]: the weights of the data-gradient
  * convolution, so that dx = unet_conv3x3_fwd(dy, wt, NULL, dx, 0). */
 UNET_API int unet_flip_weights(const void *w, void *wt, int cout, int cin,
@@ -48,6 +52,11 @@ UNET_API int unet_flip_weights(const void *w, void *wt, int cout, int cin,
  * db[co] += sum_p dy[p][co] if db != NULL. */
 UNET_API int unet_conv3x3_wgrad(const unet_act *x, const unet_act *dy, float *dw, float *db,
                                 stencil_stream_t stream);
+/* Weight gradient of the dilated convolution (taps dilation * (ky-1, kx-1));
+ * its data gradient is unet_conv3x3_fwd_dil with the flipped weights and the
+ * same dilation. */
+UNET_API int unet_conv3x3_wgrad_dil(const unet_act *x, const unet_act *dy, float *dw, float *db,
+                                    int dilation, stencil_stream_t stream);
 /* g *= (y > 0), element-wise over the view. */
 UNET_API int unet_relu_bwd(const unet_act *g, const unet_act *y, stencil_stream_t stream);
 /* 2x2 max pooling (h, w even) and its gradient (to the first maximal input). */

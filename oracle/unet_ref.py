@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import numpy as np
 
+DILATION = {"ba": 2, "bb": 4}
 LAYERS = [
     ("e0a", 32, 32), ("e0b", 32, 32), ("e1a", 32, 64), ("e1b", 64, 64),
     ("e2a", 64, 128), ("e2b", 128, 128), ("ba", 128, 256), ("bb", 256, 256),
@@ -51,7 +52,8 @@ def forward(torch, params: dict, x, head_w, head_b):
         w, b = params[name]
         cout, _, cin = w.shape
         wk = w.reshape(cout, 3, 3, cin).permute(0, 3, 1, 2)
-        return F.relu(F.conv2d(t, wk, b, padding=1))
+        d = DILATION.get(name, 1)
+        return F.relu(F.conv2d(t, wk, b, padding=d, dilation=d))
 
     e0 = conv("e0b", conv("e0a", x))
     e1 = conv("e1b", conv("e1a", F.max_pool2d(e0, 2)))

@@ -121,3 +121,28 @@ def test_ngpus_must_be_one():
         r = subprocess.run(["gcc", "-DNGPUS=2", "-I", os.path.join(ROOT, "include"), "-c", src,
                             "-o", os.path.join(tmp, "m.o")], capture_output=True, text=True)
         assert r.returncode != 0 and "NGPUS" in r.stderr
+
+
+@pytest.mark.parametrize("dims,variant,radius,block_x,threads,want", [
+    # 3-D: b0 = BLOCK_X, b1 = min(max(2, R), 8), b2 = threads / (b0 * b1), sorted descending
+    (3, "base", 1, 32, 1024, (32, 16, 2)),
+    (3, "base", 4, 32, 1024, (32, 8, 4)),
+    (3, "smem", 16, 32, 512, (32, 8, 2)),
+    (3, "base", 2, 8, 256, (16, 8, 2)),
+    # padded smem halves b0 while threads / (b0 * R * R) == 0
+    (3, "smem_padded", 8, 32, 1024, (16, 8, 8)),
+    (3, "smem_padded", 16, 64, 1024, (32, 8, 4)),
+    # 2-D: (BLOCK_X, threads / BLOCK_X, 1)
+    (2, "base", 1, 32, 1024, (32, 32, 1)),
+    (2, "smem_padded", 4, 64, 768, (64, 12, 1)),
+])
+def test_reference_heuristic_block(stencil_lib, dims, variant, radius, block_x, threads, want):
+    """stencil_heuristic_block restates src/stencil_dispatch.cu:89-101."""
+    from thesis_gb300 import lib
+    p = lib.make_params((64,) * dims, radius, 1, lib.MODE_JACOBI, variant, (block_x, 0, 0))
+    bx, by, bz = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    assert stencil_lib.stencil_heuristic_block(ctypes.byref(p), threads, ctypes.byref(bx),
+                                               ctypes.byref(by), ctypes.byref(bz)) == 0
+    assert (bx.value, by.value, bz.value) == want
+    assert stencil_lib.stencil_heuristic_block(ctypes.byref(p), 0, ctypes.byref(bx),
+                                               ctypes.byref(by), ctypes.byref(bz)) != 0

@@ -190,3 +190,57 @@ def test_temporal_blocking_full_size(cuda):
         del a, b
         torch.cuda.empty_cache()
     assert bits_equal(outs[0], outs[1]) and bits_equal(outs[0], outs[2])
+
+
+def special_values_grid(shape, seed):
+    """Uniform field with regions of -0.0, +0.0, subnormals, huge values
+    (sums overflow to inf), NaN and alternating signs, so every division path
+    and every signed-zero case of the sum meets the oracle."""
+    rng = np.random.default_rng(seed)
+    u = O.uniform(shape, seed=seed)
+    flat = u.reshape(-1)
+    n = flat.size
+    picks = rng.integers(0, 8, n)
+    flat[picks == 1] = -0.0
+    flat[picks == 2] = 0.0
+    flat[picks == 3] = np.float32(1e-39) * rng.choice([-1, 1], (picks == 3).sum())
+    flat[picks == 4] = np.float32(3e38) * rng.choice([-1, 1], (picks == 4).sum())
+    flat[picks == 5] = -flat[picks == 5]
+    flat[rng.integers(0, n, 3)] = np.nan
+    # a block of all -0.0 so that whole neighbourhoods sum -0 terms only
+    sl = tuple(slice(2, 2 + 12) for _ in shape)
+    u[sl] = -0.0
+    return u
+
+
+@pytest.mark.parametrize("shape,radius", [((40, 40, 64), 1), ((40, 40, 64), 2), ((36, 40, 72), 3),
+                                          ((36, 40, 72), 4), ((64, 96), 1), ((64, 96), 3)])
+@pytest.mark.parametrize("variant", ["base", "smem_padded", "smem_register", "coop", "cluster"])
+@pytest.mark.parametrize("mode", [O.LEGACY, O.JACOBI], ids=["legacy", "jacobi"])
+def test_special_values_match_oracle(cuda, shape, radius, variant, mode):
+    u = special_values_grid(shape, radius * 7 + len(shape))
+    got, *_ = gpu_run(u, radius, 2, mode, variant, u.copy())
+    want = oracle_run(u, radius, 2, mode, u.copy())
+    # NaN payloads differ between CPUs and GPUs (the GPU returns its canonical
+    # NaN); NaN positions and every other bit pattern must agree.
+    nan_g, nan_w = np.isnan(got), np.isnan(want)
+    assert np.array_equal(nan_g, nan_w)
+    assert np.array_equal(got[~nan_g].view(np.uint32), want[~nan_w].view(np.uint32))
+
+
+PERSISTENT_CASES = [((40, 36, 64), 1, 0), ((40, 36, 64), 1, 1), ((40, 36, 64), 1, 7),
+                    ((48, 40, 72), 2, 6), ((36, 44, 136), 3, 5), ((48, 48, 48), 4, 4),
+                    ((20, 24, 260), 1, 9), ((72, 130, 260), 2, 3)]
+
+
+@pytest.mark.parametrize("case", PERSISTENT_CASES, ids=lambda c: "x".join(map(str, c[0])) + "_r%d_i%d" % c[1:])
+@pytest.mark.parametrize("mode", [O.LEGACY, O.JACOBI], ids=["legacy", "jacobi"])
+def test_persistent_stream_matches_oracle(cuda, case, mode):
+    """COOP with temporal = 1: every sweep in one cooperative launch, a
+    grid-wide barrier between sweeps; bit-exact, result buffer by parity."""
+    shape, radius, iters = case
+    u = O.uniform(shape, seed=31 + radius)
+    second = O.uniform(shape, seed=32) if mode == O.LEGACY else None
+    got, u1, u2, res = gpu_run(u, radius, iters, mode, "coop", second, temporal=1)
+    assert (res.data_ptr() == u1.data_ptr()) == (iters % 2 == 0)
+    assert bits_equal(got, oracle_run(u, radius, iters, mode, second))

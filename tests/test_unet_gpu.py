@@ -17,9 +17,10 @@ def _nhwc_to_nchw(t):
     return t.permute(0, 3, 1, 2)
 
 
-@pytest.mark.parametrize("cin,cout,h,w", [(32, 64, 16, 24), (64, 32, 8, 8), (96, 32, 12, 20),
-                                          (384, 128, 8, 16)])
-def test_conv3x3_fwd_dgrad_wgrad(cuda, cin, cout, h, w):
+@pytest.mark.parametrize("cin,cout,h,w,dil", [(32, 64, 16, 24, 1), (64, 32, 8, 8, 1), (96, 32, 12, 20, 1),
+                                              (384, 128, 8, 16, 1), (128, 256, 16, 16, 2),
+                                              (256, 256, 16, 12, 4), (32, 32, 6, 10, 4)])
+def test_conv3x3_fwd_dgrad_wgrad(cuda, cin, cout, h, w, dil):
     import torch
     from thesis_gb300 import unet as U
     L = U._L()
@@ -31,11 +32,12 @@ def test_conv3x3_fwd_dgrad_wgrad(cuda, cin, cout, h, w):
     dy = torch.randn(n, h, w, cout, generator=g).to(torch.bfloat16)
     xd, wd, bd, dyd = x.cuda(), wt.cuda(), b.cuda(), dy.cuda()
     y = torch.empty(n, h, w, cout, dtype=torch.bfloat16, device="cuda")
-    U._chk(L.unet_conv3x3_fwd(ctypes.byref(U.view(xd)), U._p(wd), U._p(bd), ctypes.byref(U.view(y)), 1, None), "fwd")
+    U._chk(L.unet_conv3x3_fwd_dil(ctypes.byref(U.view(xd)), U._p(wd), U._p(bd), ctypes.byref(U.view(y)), 1, dil,
+                                  None), "fwd")
     # reference in float64 on the same BF16 inputs
     X = _nhwc_to_nchw(x.double()).requires_grad_(True)
     W = wt.double().reshape(cout, 3, 3, cin).permute(0, 3, 1, 2).contiguous().requires_grad_(True)
-    pre = torch.nn.functional.conv2d(X, W, b.double(), padding=1)
+    pre = torch.nn.functional.conv2d(X, W, b.double(), padding=dil, dilation=dil)
     Y = torch.relu(pre)
     got = _nhwc_to_nchw(y.cpu().double())
     err = (got - Y).abs().max().item() / Y.abs().max().item()
@@ -44,10 +46,12 @@ def test_conv3x3_fwd_dgrad_wgrad(cuda, cin, cout, h, w):
     wflip = torch.empty(cin, 9, cout, dtype=torch.bfloat16, device="cuda")
     U._chk(L.unet_flip_weights(U._p(wd), U._p(wflip), cout, cin, None), "flip")
     dx = torch.empty(n, h, w, cin, dtype=torch.bfloat16, device="cuda")
-    U._chk(L.unet_conv3x3_fwd(ctypes.byref(U.view(dyd)), U._p(wflip), None, ctypes.byref(U.view(dx)), 0, None), "dgrad")
+    U._chk(L.unet_conv3x3_fwd_dil(ctypes.byref(U.view(dyd)), U._p(wflip), None, ctypes.byref(U.view(dx)), 0, dil,
+                                  None), "dgrad")
     dw = torch.zeros(cout, 9, cin, device="cuda")
     db = torch.zeros(cout, device="cuda")
-    U._chk(L.unet_conv3x3_wgrad(ctypes.byref(U.view(xd)), ctypes.byref(U.view(dyd)), U._p(dw), U._p(db), None), "wgrad")
+    U._chk(L.unet_conv3x3_wgrad_dil(ctypes.byref(U.view(xd)), ctypes.byref(U.view(dyd)), U._p(dw), U._p(db), dil,
+                                    None), "wgrad")
     pre.backward(_nhwc_to_nchw(dy.double()))
     gx = _nhwc_to_nchw(dx.cpu().double())
     assert (gx - X.grad).abs().max().item() / X.grad.abs().max().item() < 1e-2
@@ -97,7 +101,7 @@ def test_network_gradients_match_cpu_reference(cuda):
     import torch
     from oracle import unet_ref as R
     from thesis_gb300 import stencil as S, unet as U
-    n, h, w = 2, 32, 32
+    n, h, w = 2, 64, 64
     fields = torch.stack([S.init_laplace2d((h, w), 100 + k) for k in range(n)])
     target = torch.randn(n, h, w, device="cuda") * 0.1
     net = U.UNet(seed=7)

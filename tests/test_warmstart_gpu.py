@@ -24,8 +24,11 @@ def test_training_reduces_loss_and_network_beats_zero_init(cuda):
     r_zero = W.residuals(zero)
     sw_zero, _ = W.sweeps_to_tol(zero, 1e-5, chunk=500)
     sw_net, _ = W.sweeps_to_tol(list(pred), 1e-5, chunk=500)
-    print("sweeps zero %s net %s" % (np.mean(sw_zero), np.mean(sw_net)))
+    # ablation: the same pipeline without the network (its Coons base field)
+    sw_coons, _ = W.sweeps_to_tol(list(W.coons_fill(f)), 1e-5, chunk=500)
+    print("sweeps zero %s coons %s net %s" % (np.mean(sw_zero), np.mean(sw_coons), np.mean(sw_net)))
     assert np.mean(sw_net) < np.mean(sw_zero)
+    assert np.mean(sw_net) < np.mean(sw_coons)
     # fallback rule inputs are well defined
     r_net = W.residuals(list(pred))
     assert all(np.isfinite(r_net)) and all(np.isfinite(r_zero))

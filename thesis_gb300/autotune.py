@@ -59,8 +59,10 @@ def variant_space(shape, radius):
         if dims == 3 and radius <= 4:
             top.append({"variant": "smem_register"})
             # default shape, 64 x 32 tiles, one row per thread, 16-slot ring,
-            # and (nx % 128 == 0, nx <= 512) the full-width row-slab kernel
+            # 128 x 32 tiles (R <= 2) or 16 one-row warps (R >= 3), and
+            # (nx % 128 == 0, nx <= 512) the full-width row-slab kernel
             sub["smem_register"] = {"block": [(0, 0, 0), (16, 32, 1), (0, 1, 0), (0, 0, 3),
+                                              (0, 0, 5 if radius <= 2 else 4),
                                               (0, 8, 0), (0, 8, 1)]}
         if radius <= 4:
             top.append({"variant": "cluster"})

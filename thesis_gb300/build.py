@@ -69,5 +69,36 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     return LIB
 
 
+MAIN_SRC = os.path.join(HERE, "host", "stencil_main.c")
+BIN = os.path.join(HERE, "bin")
+
+
+def main_name(defines: dict) -> str:
+    """bin/stencil_<...> named by the configuration's -D values."""
+    tag = "_".join("%s%s" % (k.lower(), v) for k, v in sorted(defines.items()))
+    return os.path.join(BIN, "stencil_" + (tag or "default"))
+
+
+def build_main(defines: dict | None = None, out: str | None = None) -> str:
+    """Compiles the drop-in stencil binary (host/stencil_main.c) for one
+    compile-time configuration, given as the reference's -D macros (DIM,
+    DIMENSIONS, RADIUS, ITERATIONS, SMEM, PADDED, REGISTER, COOP, BLOCK_X, ...),
+    and links it to the in-tree library (gcc only: the binary calls the C ABI
+    and needs no CUDA headers or libraries of its own)."""
+    defines = dict(defines or {})
+    build()
+    out = out or main_name(defines)
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    cmd = (["gcc", "-O2", "-std=c99", "-Wall", "-I", INCLUDE] +
+           ["-D%s=%s" % (k, v) for k, v in sorted(defines.items())] +
+           [MAIN_SRC, "-o", out + ".tmp", "-L", HERE, "-lstencil_gb300",
+            "-Wl,-rpath," + HERE, "-lm"])
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("stencil_main build failed:\n%s%s" % (res.stdout, res.stderr))
+    os.replace(out + ".tmp", out)
+    return out
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv))

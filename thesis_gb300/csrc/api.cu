@@ -25,6 +25,8 @@ int run_rows3d(const Geom &g, float *a, float *b, int iters, int shape, cudaStre
                float **res);
 
 static thread_local char t_err[512];
+static thread_local long long t_launches = 0;
+static thread_local const char *t_engine = "none";
 
 int fail(int code, const char *fmt, ...) {
     va_list ap;
@@ -125,7 +127,7 @@ struct DeviceWorkspace {
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 static std::mutex g_ws_mu;
@@ -135,8 +137,7 @@ static int ws_grids(int dev, size_t bytes, DeviceWorkspace **out) {
     DeviceWorkspace &w = g_ws[dev];
     if (!w.stream) {
         ST_CUDA(cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking));
-        ST_CUDA(cudaEventCreate(&w.ev[0]));
-        ST_CUDA(cudaEventCreate(&w.ev[1]));
+        for (auto &e : w.ev) ST_CUDA(cudaEventCreate(&e));
     }
     if (w.grid_bytes < bytes) {
         cudaStreamSynchronize(w.stream);
@@ -195,6 +196,11 @@ static bool tuned_choice(const stencil_params &p, stencil_params *out) {
 // Variant choice when the caller leaves it to the library: grids that fit a
 // cluster's shared memory run all sweeps in one cluster launch (launch- and
 // sync-bound otherwise); large 3-D grids stream; the rest use the base kernel.
+void note_launches(const char *engine, long long n) {
+    if (!t_launches) t_engine = engine;
+    t_launches += n;
+}
+
 static int choose_variant(const stencil_params &p) {
     const Geom g = make_geom(p);
     if (p.iterations >= 8 && cluster_resident(g, p.dims)) return STENCIL_VARIANT_CLUSTER;
@@ -253,6 +259,8 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const Geom g = make_geom(*p);
     float *cur = d_u1, *nxt = d_u2;
+    t_launches = 0;
+    t_engine = "none";
     if (d_result) *d_result = cur;
     if (p->iterations == 0) return STENCIL_OK;
     int variant = p->variant;
@@ -268,7 +276,8 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
         if (!q.temporal) q.temporal = tuned.temporal;
         if (q.variant != STENCIL_VARIANT_AUTO) return stencil_dispatch_ex(&q, d_u1, d_u2, stream, d_result);
     }
-    if (variant == STENCIL_VARIANT_AUTO) variant = choose_variant(*p);
+    const bool auto_pick = variant == STENCIL_VARIANT_AUTO;
+    if (auto_pick) variant = choose_variant(*p);
     if (variant == STENCIL_VARIANT_SMEM_REGISTER && !(p->dims == 3 && stream3d_supported(g)))
         variant = STENCIL_VARIANT_SMEM_PADDED;
     if ((variant == STENCIL_VARIANT_SMEM || variant == STENCIL_VARIANT_SMEM_PADDED) &&
@@ -294,9 +303,16 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
         if (d_result) *d_result = res;
         return STENCIL_OK;
     }
-    if (variant == STENCIL_VARIANT_COOP)
-        variant = p->dims == 3 && stream3d_supported(g) ? STENCIL_VARIANT_SMEM_REGISTER
-                                                        : STENCIL_VARIANT_BASE;
+    if (variant == STENCIL_VARIANT_COOP && p->dims == 3 && stream3d_supported(g)) {
+        // One sweep per HBM pass, all sweeps in one persistent cooperative
+        // launch with a grid-wide barrier between them.
+        float *res = nullptr;
+        rc = run_stream3d(g, cur, nxt, p->iterations, 0, 0, s, &res, 0, true);
+        if (rc) return rc;
+        if (d_result) *d_result = res;
+        return STENCIL_OK;
+    }
+    if (variant == STENCIL_VARIANT_COOP) variant = STENCIL_VARIANT_BASE;
     if (variant == STENCIL_VARIANT_SMEM_REGISTER && p->block_x == 0 && p->block_y == 8 &&
         rows3d_supported(g)) {
         float *res = nullptr;
@@ -306,13 +322,18 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
         return STENCIL_OK;
     }
     if (variant == STENCIL_VARIANT_SMEM_REGISTER) {
+        // Left to the library (no tile shape given): all sweeps in one
+        // persistent launch, at least as fast as a launch per sweep (512^3:
+        // equal at R = 1, +4 % at R = 4; 256^3: +8 %).
+        const bool persistent = auto_pick && !p->block_x && !p->block_y && !p->block_z;
         float *res = nullptr;
         rc = run_stream3d(g, cur, nxt, p->iterations, p->block_x ? 4 * p->block_x : 0,
-                          p->block_y, s, &res, p->block_z);
+                          p->block_y, s, &res, p->block_z, persistent);
         if (rc) return rc;
         if (d_result) *d_result = res;
         return STENCIL_OK;
     }
+    note_launches(variant == STENCIL_VARIANT_BASE ? "base" : "tile", p->iterations);
     for (int it = 0; it < p->iterations; ++it) {
         if (variant == STENCIL_VARIANT_BASE)
             rc = launch_base_sweep(g, p->dims, cur, nxt, p->block_x, p->block_y, p->block_z,
@@ -326,7 +347,8 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
     return STENCIL_OK;
 }
 
-int stencil_run_host(const stencil_params *p, const float *h_in, float *h_out, float *ms) {
+int stencil_run_host_timed(const stencil_params *p, const float *h_in, float *h_out,
+                           float *ms_total, float *ms_sweeps) {
     int rc = stencil_params_check(p);
     if (rc) return rc;
     if (!h_in || !h_out) return fail(STENCIL_EINVAL, "null host buffer");
@@ -344,17 +366,24 @@ int stencil_run_host(const stencil_params *p, const float *h_in, float *h_out, f
     else
         ST_CUDA(cudaMemsetAsync(w->u[1], 0, bytes, w->stream));
     float *res = nullptr;
+    ST_CUDA(cudaEventRecord(w->ev[2], w->stream));
     rc = stencil_dispatch_ex(p, w->u[0], w->u[1], reinterpret_cast<stencil_stream_t>(w->stream),
                              &res);
     if (rc) {
         cudaStreamSynchronize(w->stream);
         return rc;
     }
+    ST_CUDA(cudaEventRecord(w->ev[3], w->stream));
     ST_CUDA(cudaMemcpyAsync(h_out, res, bytes, cudaMemcpyDeviceToHost, w->stream));
     ST_CUDA(cudaEventRecord(w->ev[1], w->stream));
     ST_CUDA(cudaStreamSynchronize(w->stream));
-    if (ms) ST_CUDA(cudaEventElapsedTime(ms, w->ev[0], w->ev[1]));
+    if (ms_total) ST_CUDA(cudaEventElapsedTime(ms_total, w->ev[0], w->ev[1]));
+    if (ms_sweeps) ST_CUDA(cudaEventElapsedTime(ms_sweeps, w->ev[2], w->ev[3]));
     return STENCIL_OK;
+}
+
+int stencil_run_host(const stencil_params *p, const float *h_in, float *h_out, float *ms) {
+    return stencil_run_host_timed(p, h_in, h_out, ms, nullptr);
 }
 
 int stencil_init_reference(const stencil_params *p, float *d_u, stencil_stream_t stream) {
@@ -452,6 +481,12 @@ const char *stencil_strerror(int status) {
 
 const char *stencil_last_error(void) { return t_err; }
 
+int stencil_last_dispatch(const char **engine, long long *kernel_launches) {
+    if (engine) *engine = t_engine;
+    if (kernel_launches) *kernel_launches = t_launches;
+    return STENCIL_OK;
+}
+
 int stencil_device_status(int *status) {
     if (!status) return fail(STENCIL_EINVAL, "null pointer");
     ST_CUDA(cudaDeviceSynchronize());
@@ -475,6 +510,28 @@ int stencil_release(void) {
     if (w.ev[1]) cudaEventDestroy(w.ev[1]);
     if (w.stream) cudaStreamDestroy(w.stream);
     w = DeviceWorkspace();
+    return STENCIL_OK;
+}
+
+int stencil_heuristic_block(const stencil_params *p, int threads, int *bx, int *by, int *bz) {
+    if (!p || !bx || !by || !bz) return fail(STENCIL_EINVAL, "null argument");
+    if (p->block_x < 1 || threads < 1 || threads > 1024 || p->radius < 1 ||
+        (p->dims != 2 && p->dims != 3))
+        return fail(STENCIL_EINVAL, "heuristic needs dims 2/3, radius >= 1, block_x >= 1, 1..1024 threads");
+    if (p->dims == 3) {
+        int b0 = p->block_x;
+        const bool padded = p->variant == STENCIL_VARIANT_SMEM_PADDED;
+        while (padded && threads / (b0 * p->radius * p->radius) == 0 && b0 > 1) b0 /= 2;
+        int b1 = std::min(std::max(2, p->radius), 8);
+        int b2 = threads / (b0 * b1);
+        // descending order of the three extents
+        if (b0 < b2) std::swap(b0, b2);
+        if (b0 < b1) std::swap(b0, b1);
+        if (b1 < b2) std::swap(b1, b2);
+        *bx = b0, *by = b1, *bz = b2;
+    } else {
+        *bx = p->block_x, *by = threads / p->block_x, *bz = 1;
+    }
     return STENCIL_OK;
 }
 

@@ -92,6 +92,58 @@ __device__ __forceinline__ float div_coeff(float x) {
     return div_fast_ok<C>(x) ? div_fast<C>(x) : x / (float)C;
 }
 
+// ---------------------------------------------------------------------------
+// Packed FP32 pairs (sm_100 family: add/mul/fma.rn.f32x2).  Each element is
+// rounded exactly as the scalar instruction would round it (IEEE round to
+// nearest, subnormals kept), so a sum built from pairs is bit-identical to
+// the scalar sum in the same order; one instruction does two cells' work.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 fadd2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "mov.b64 rc, {%6, %7};\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+
+// div_fast on a pair (the same three roundings per element; -q0*c + x is
+// formed as q0*(-c) + x, the negation being exact).
+template <int C>
+__device__ __forceinline__ float2 div_fast2(float2 x) {
+    constexpr float rc = 1.0f / (float)C;
+    if ((C & (C - 1)) == 0) return fmul2(x, make_float2(rc, rc));
+    const float2 q0 = fmul2(x, make_float2(rc, rc));
+    const float2 r = ffma2(q0, make_float2(-(float)C, -(float)C), x);
+    return ffma2(r, make_float2(rc, rc), q0);
+}
+
+// Division of a sum that was started from its first term instead of +0.0f:
+// the two differ only for an all-(-0) sum (-0 here, +0 in the reference), and
+// x + 0.0f maps exactly that case to +0 and leaves every other value as is.
+template <int C>
+__device__ __forceinline__ float div_slow_from_first(float x) {
+    return (x + 0.0f) / (float)C;
+}
+
 template <int D, int R>
 __device__ __forceinline__ float star_finish(float acc, float centre, int legacy) {
     const float v = div_coeff<2 * D * R>(acc);
@@ -169,6 +221,51 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
             return false;
         }
     }
+    return true;
+}
+
+// Named barrier `id` over `count` threads (a multiple of 32) that also ANDs a
+// predicate, so that a failed bounded wait in one warp ends all of them
+// together.
+__device__ __forceinline__ bool named_barrier_and(int id, int count, bool ok) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred p, %2, %3, p;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)ok), "r"(id), "r"(count)
+        : "memory");
+    return r != 0;
+}
+
+// Grid-wide barrier of a cooperative launch (all CTAs co-resident), on a
+// counter that the host zeroes before the launch.  A CTA arrives once its
+// threads have passed a CTA-level barrier after their last stores: a fence,
+// then a release add at GPU scope.  A waiter spins with acquire loads until
+// the counter reaches the target (a bounded wait), then orders what it
+// acquired before its own later TMA (async-proxy) reads.
+__device__ __forceinline__ void grid_arrive(unsigned *ctr) {
+    __threadfence();
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(ctr) : "memory");
+}
+
+__device__ __forceinline__ bool grid_wait_bounded(const unsigned *ctr, unsigned target,
+                                                  uint64_t limit_ns = kWaitLimitNs) {
+    unsigned v;
+    uint64_t t0 = 0;
+    for (;;) {
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+        if (v >= target) break;
+        const uint64_t t = globaltimer_ns();
+        if (!t0) t0 = t;
+        else if (t - t0 > limit_ns) {
+            report_status(kStatusTimeout);
+            return false;
+        }
+    }
+    asm volatile("fence.proxy.async.global;" ::: "memory");
     return true;
 }
 

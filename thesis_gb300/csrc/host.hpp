@@ -40,8 +40,13 @@ int launch_tile_sweep(const Geom &g, int dims, const float *src, float *dst, int
 // Multi-sweep drivers: run `iters` sweeps ping-ponging between a and b
 // starting from a; *res receives the buffer holding the final state.
 // shape_hint (block_z of the parameters): 0 = by tile fields, 1..3 = a shape.
+// Records kernel launches of the current dispatch (stencil_last_dispatch).
+void note_launches(const char *engine, long long n);
+bool stream3d_supported(const Geom &g);
+// persistent: all sweeps in one cooperative launch with a grid barrier
+// between sweeps (default shape of each radius) instead of one launch each.
 int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int tile_y,
-                 cudaStream_t s, float **res, int shape_hint = 0);
+                 cudaStream_t s, float **res, int shape_hint = 0, bool persistent = false);
 int run_tb3d(const Geom &g, float *a, float *b, int iters, int temporal, cudaStream_t s,
              float **res);
 // All sweeps of one grid on one thread-block cluster (k_cluster.cu).

@@ -495,6 +495,7 @@ int run_cluster(const Geom &g, int dims, float *a, float *b, int iters, cudaStre
     const ClusterJob *none = nullptr;
     unsigned *noq = nullptr;
     ST_CUDA(cudaLaunchKernelEx(&cfg, k_cluster, j, none, 1, noq));
+    note_launches("cluster", 1);
     if (res) *res = (iters & 1) ? b : a;
     return STENCIL_OK;
 }
@@ -522,18 +523,33 @@ struct BatchHeader {
     int clusters;
 };
 
-// Launch shape of each prepared workspace (set by prepare, read by launch).
-std::mutex g_batch_mu;
-std::vector<std::pair<const void *, BatchHeader>> g_batch;
+// A 3-D job too large for a cluster's shared memory: swept by the whole GPU
+// (the persistent stream kernel, one cooperative launch per job) after the
+// cluster jobs, instead of by one 16-SM cluster from L2/HBM (about twice the
+// throughput on the 128-grid benchmark batch).
+struct StreamedJob {
+    Geom g;
+    float *a, *b;
+    int iters;
+};
 
-void remember(const void *ws, const BatchHeader &h) {
+struct BatchPlan {
+    BatchHeader h;                    // the cluster part (njobs = cluster jobs)
+    std::vector<StreamedJob> streamed;
+};
+
+// Launch plan of each prepared workspace (set by prepare, read by launch).
+std::mutex g_batch_mu;
+std::vector<std::pair<const void *, BatchPlan>> g_batch;
+
+void remember(const void *ws, const BatchPlan &h) {
     std::lock_guard<std::mutex> lock(g_batch_mu);
     for (auto &c : g_batch)
         if (c.first == ws) { c.second = h; return; }
     g_batch.emplace_back(ws, h);
 }
 
-bool recall(const void *ws, BatchHeader *h) {
+bool recall(const void *ws, BatchPlan *h) {
     std::lock_guard<std::mutex> lock(g_batch_mu);
     for (auto &c : g_batch)
         if (c.first == ws) { *h = c.second; return true; }
@@ -573,6 +589,7 @@ extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, i
     const int csize = cluster_size ? cluster_size : cluster_size_for_device();
     std::vector<ClusterJob> table;
     std::vector<double> work;
+    BatchPlan plan;
     table.reserve(njobs);
     for (int i = 0; i < njobs; ++i) {
         const stencil_batch_job &b = jobs[i];
@@ -587,43 +604,58 @@ extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, i
             return fail(STENCIL_EINVAL, "job %d: two distinct 16-byte aligned buffers required", i);
         if (!cluster_job_ok(b.dims, b.nx, b.ny, b.nz, b.radius))
             return fail(STENCIL_EUNSUPPORTED, "job %d: batch jobs need nx %% 4 == 0 and radius <= 4", i);
-        table.push_back(make_job(make_geom(p), p.dims, b.d_u1, b.d_u2, b.iterations, csize));
+        const Geom g = make_geom(p);
+        ClusterJob j = make_job(g, p.dims, b.d_u1, b.d_u2, b.iterations, csize);
+        if (p.dims == 3 && !j.resident && stream3d_supported(g)) {
+            plan.streamed.push_back({g, b.d_u1, b.d_u2, b.iterations});
+            continue;
+        }
+        table.push_back(j);
         work.push_back((double)cell_count(p) * b.iterations);
     }
+    const int nc = (int)table.size();
     // Largest job first: the queue hands them out in this order.
-    std::vector<int> order(njobs);
-    for (int i = 0; i < njobs; ++i) order[i] = i;
+    std::vector<int> order(nc);
+    for (int i = 0; i < nc; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
-    std::vector<ClusterJob> sorted(njobs);
-    for (int i = 0; i < njobs; ++i) sorted[i] = table[order[i]];
-    BatchHeader h;
+    std::vector<ClusterJob> sorted(nc);
+    for (int i = 0; i < nc; ++i) sorted[i] = table[order[i]];
+    BatchHeader &h = plan.h;
     h.queue = 0;
-    h.njobs = njobs;
+    h.njobs = nc;
     h.cluster_size = csize;
     h.clusters = max_active_clusters(csize);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const size_t hb = (sizeof(BatchHeader) + 255) & ~(size_t)255;
     char *ws = static_cast<char *>(d_workspace);
     ST_CUDA(cudaMemcpyAsync(ws, &h, sizeof h, cudaMemcpyHostToDevice, s));
-    if (njobs)
-        ST_CUDA(cudaMemcpyAsync(ws + hb, sorted.data(), njobs * sizeof(ClusterJob),
+    if (nc)
+        ST_CUDA(cudaMemcpyAsync(ws + hb, sorted.data(), nc * sizeof(ClusterJob),
                                 cudaMemcpyHostToDevice, s));
     ST_CUDA(cudaStreamSynchronize(s));
-    remember(d_workspace, h);
+    remember(d_workspace, plan);
     return STENCIL_OK;
 }
 
 extern "C" int stencil_batch_launch(const void *d_workspace, stencil_stream_t stream) {
     if (!d_workspace) return fail(STENCIL_EINVAL, "null workspace");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    BatchHeader h{};
-    if (!recall(d_workspace, &h))
+    BatchPlan plan;
+    if (!recall(d_workspace, &plan))
         return fail(STENCIL_EINVAL, "workspace was not prepared by stencil_batch_prepare");
-    if (h.njobs == 0) return STENCIL_OK;
-    const size_t hb = (sizeof(BatchHeader) + 255) & ~(size_t)255;
-    const ClusterJob *table = reinterpret_cast<const ClusterJob *>(static_cast<const char *>(d_workspace) + hb);
-    unsigned *queue = reinterpret_cast<unsigned *>(const_cast<void *>(d_workspace));
-    return launch_cluster_jobs(table, h.njobs, queue, std::min(h.clusters, h.njobs), h.cluster_size, s);
+    const BatchHeader &h = plan.h;
+    if (h.njobs) {
+        const size_t hb = (sizeof(BatchHeader) + 255) & ~(size_t)255;
+        const ClusterJob *table = reinterpret_cast<const ClusterJob *>(static_cast<const char *>(d_workspace) + hb);
+        unsigned *queue = reinterpret_cast<unsigned *>(const_cast<void *>(d_workspace));
+        int rc = launch_cluster_jobs(table, h.njobs, queue, std::min(h.clusters, h.njobs), h.cluster_size, s);
+        if (rc) return rc;
+    }
+    for (const StreamedJob &j : plan.streamed) {
+        int rc = run_stream3d(j.g, j.a, j.b, j.iters, 0, 0, s, nullptr, 0, true);
+        if (rc) return rc;
+    }
+    return STENCIL_OK;
 }
 
 extern "C" int stencil_batch_forget(const void *d_workspace) {

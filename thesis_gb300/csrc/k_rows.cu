@@ -290,6 +290,7 @@ int run_rows3d(const Geom &g, float *a, float *b, int iters, int shape, cudaStre
     const int grid = std::min(items, resident);
     float *cur = a, *nxt = b;
     Geom gg = g;
+    note_launches("rows3d", iters);
     for (int it = 0; it < iters; ++it) {
         const float *src = cur;
         void *args[] = {&src, &nxt, &gg, &zchunk, &items};

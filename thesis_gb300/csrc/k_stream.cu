@@ -28,6 +28,9 @@
 // sequence number fixes each plane's slot and mbarrier phase.  No CTA-wide
 // barrier is used after set-up, and every mbarrier wait is bounded.
 #include <algorithm>
+#include <atomic>
+#include <mutex>
+#include <vector>
 #include <cmath>
 
 #include "host.hpp"
@@ -46,6 +49,12 @@ struct StreamShape {
     static constexpr int CWARPS = CONSUMERS / 32;
     static constexpr int THREADS = CONSUMERS + 32;
     static constexpr int SMEM_BYTES = NS * SLOT_FLOATS * 4 + 128 + 2 * NS * 8;
+    // Two resident CTAs where the registers allow: the 8-slot R = 1 shapes
+    // of 9 warps, or of 17 one-row warps (56 registers), and the
+    // one-row-per-thread 9-warp shapes at larger radii (their budget, 96 to
+    // 112 registers, holds the 2R+1-plane queue of one row).
+    static constexpr int MIN_BLOCKS =
+        ((R <= 1 && NS <= 8 && (THREADS <= 320 || RY == 1)) || (RY == 1 && THREADS <= 320)) ? 2 : 1;
     static_assert(PW <= 256 && PH <= 256, "TMA box dimensions are limited to 256");
     static_assert(TX % 4 == 0 && TY % RY == 0 && CONSUMERS % 32 == 0, "bad tile");
     static_assert((NS & (NS - 1)) == 0 && NS >= R + 2, "ring must be a power of two > R+1");
@@ -53,20 +62,42 @@ struct StreamShape {
 
 __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 
-template <int R, int TX, int TY, int RY, int NS>
-__global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <= 1 && NS <= 8 ? 2 : 1))
-    k_stream3d(const __grid_constant__ CUtensorMap src_map, float *__restrict__ dst, Geom g,
-               int tiles_x, int tiles_y, int zchunk, int items) {
+// Sums of two cells at a time: packed f32x2 instructions where the kernel is
+// issue-bound (R >= 3: 467 vs 412 GCell/s at 512^3, R = 4), scalar ones where
+// it is bandwidth-bound (R = 1: 691 scalar vs 627 packed) -- the same
+// roundings either way.
+template <bool PK>
+__device__ __forceinline__ float2 add_pair(float2 a, float2 b) {
+    if constexpr (PK) return fadd2(a, b);
+    else return make_float2(a.x + b.x, a.y + b.y);
+}
+template <bool PK, int C>
+__device__ __forceinline__ float2 div_pair(float2 a) {
+    if constexpr (PK) return div_fast2<C>(a);
+    else return make_float2(div_fast<C>(a.x), div_fast<C>(a.y));
+}
+
+// MULTI: one cooperative launch runs `sweeps` sweeps, ping-ponging between
+// (map0 -> dst0) and (map1 -> dst1), with a grid-wide barrier on *grid_bar
+// between sweeps; otherwise one sweep map0 -> dst0.
+template <int R, int TX, int TY, int RY, int NS, bool MULTI>
+__global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, StreamShape<R, TX, TY, RY, NS>::MIN_BLOCKS)
+    k_stream3d(const __grid_constant__ CUtensorMap map0, const __grid_constant__ CUtensorMap map1,
+               float *dst0, float *dst1, Geom g, int tiles_x, int tiles_y, int zchunk, int items,
+               int sweeps, unsigned *grid_bar) {
     using S = StreamShape<R, TX, TY, RY, NS>;
     constexpr int C = 6 * R;  // 2*D*R with D = 3
+    constexpr bool PK = R >= 3;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float *ring = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
                                             ~static_cast<uintptr_t>(127));
     uint64_t *full = reinterpret_cast<uint64_t *>(ring + NS * S::SLOT_FLOATS);
     uint64_t *empty = full + NS;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (!MULTI) sweeps = 1;
     if (tid == 0) {
-        prefetch_tensormap(&src_map);
+        prefetch_tensormap(&map0);
+        if (MULTI) prefetch_tensormap(&map1);
         for (int s = 0; s < NS; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], S::CWARPS);
@@ -80,18 +111,23 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
         // ---------------- producer ----------------
         if (lane != 0) return;
         uint32_t q = 0;
-        for (int item = blockIdx.x; item < items; item += gridDim.x) {
-            const int t = item % ntiles, ch = item / ntiles;
-            const int x0 = (t % tiles_x) * TX, y0 = (t / tiles_x) * TY;
-            const int z0 = R + ch * zchunk, z1 = min(z0 + zchunk, g.nz - R);
-            const int np = (z1 - z0) + 2 * R;
-            for (int p = 0; p < np; ++p, ++q) {
-                const int s = q & (NS - 1);
-                const uint32_t use = q / NS;
-                if (use > 0 && !mbar_wait_bounded(&empty[s], (use - 1) & 1)) return;
-                mbar_arrive_expect_tx(&full[s], S::PLANE_BYTES);
-                tma_load_3d(ring + s * S::SLOT_FLOATS, &src_map, &full[s], x0 - S::RA, y0 - R,
-                            z0 - R + p);
+        for (int sw = 0; sw < sweeps; ++sw) {
+            // Sweep sw reads what every CTA wrote in sweep sw-1.
+            if (MULTI && sw > 0 && !grid_wait_bounded(grid_bar, (unsigned)sw * gridDim.x)) return;
+            const CUtensorMap *src_map = (sw & 1) ? &map1 : &map0;
+            for (int item = blockIdx.x; item < items; item += gridDim.x) {
+                const int t = item % ntiles, ch = item / ntiles;
+                const int x0 = (t % tiles_x) * TX, y0 = (t / tiles_x) * TY;
+                const int z0 = R + ch * zchunk, z1 = min(z0 + zchunk, g.nz - R);
+                const int np = (z1 - z0) + 2 * R;
+                for (int p = 0; p < np; ++p, ++q) {
+                    const int s = q & (NS - 1);
+                    const uint32_t use = q / NS;
+                    if (use > 0 && !mbar_wait_bounded(&empty[s], (use - 1) & 1)) return;
+                    mbar_arrive_expect_tx(&full[s], S::PLANE_BYTES);
+                    tma_load_3d(ring + s * S::SLOT_FLOATS, src_map, &full[s], x0 - S::RA, y0 - R,
+                                z0 - R + p);
+                }
             }
         }
         return;
@@ -106,7 +142,10 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
     constexpr int QN = 2 * R + 1;
     float4 qz[RY][QN];  // z register queue, rotated by unrolling: plane z+k-R sits at index (z-z0+k) % QN
     uint32_t qb = 0;    // sequence number of plane 0 of the current item
-    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    bool ok = true;     // false once a bounded wait gave up
+    for (int sw = 0; sw < sweeps && ok; ++sw) {
+    float *dst = (sw & 1) ? dst1 : dst0;
+    for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
         const int t = item % ntiles, ch = item / ntiles;
         const int x0 = (t % tiles_x) * TX, y0 = (t / tiles_x) * TY;
         const int z0 = R + ch * zchunk, z1 = min(z0 + zchunk, g.nz - R);
@@ -125,15 +164,16 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
         for (int p = 0; p < 2 * R; ++p) {
             const uint32_t q = qb + p;
             const int s = q & (NS - 1);
-            if (!mbar_wait_bounded(&full[s], (q / NS) & 1)) return;
+            if (!mbar_wait_bounded(&full[s], (q / NS) & 1)) { ok = false; break; }
             const float *sl = ring + s * S::SLOT_FLOATS + own;
 #pragma unroll
             for (int r = 0; r < RY; ++r) qz[r][p] = lds4(sl + r * S::PW);
             if (p < R || p >= np - R) release(s);
         }
+        if (!ok) break;
         float *drow = dst + (long long)z0 * g.sz + (long long)ybase * g.sy + x;
         const float *ring_own = ring + own;
-        for (int zb = z0; zb < z1; zb += QN) {
+        for (int zb = z0; zb < z1 && ok; zb += QN) {
 #pragma unroll
             for (int ph = 0; ph < QN; ++ph) {
                 const int z = zb + ph;
@@ -145,7 +185,9 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
                 float4 col[RY + 2 * R];  // the thread's 4 columns, rows -R .. RY-1+R
 #pragma unroll
                 for (int k = 0; k < RY + 2 * R; ++k) col[k] = lds4(cb + (k - R) * S::PW);
-                float acc[RY][4];
+                // Sums of cells (0, 1) and (2, 3) of each row as pairs (add_pair),
+                // started from the first term (div_slow_from_first).
+                float2 acc[RY][2];
 #pragma unroll
                 for (int r = 0; r < RY; ++r) {
                     float w[4 + 2 * S::RA];
@@ -159,27 +201,37 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
                     }
                     const float4 c = col[r + R];
                     w[S::RA] = c.x; w[S::RA + 1] = c.y; w[S::RA + 2] = c.z; w[S::RA + 3] = c.w;
+                    // axis i: an even offset reads aligned pairs of the
+                    // loaded vectors (pair adds), an odd one straddles them
+                    // (scalar adds)
+                    acc[r][0] = make_float2(w[S::RA - R], w[S::RA - R + 1]);
+                    acc[r][1] = make_float2(w[S::RA - R + 2], w[S::RA - R + 3]);
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) acc[r][e] = 0.0f;
-                    // axis i
-#pragma unroll
-                    for (int o = -R; o <= R; ++o) {
+                    for (int o = -R + 1; o <= R; ++o) {
                         if (o == 0) continue;
-#pragma unroll
-                        for (int e = 0; e < 4; ++e) acc[r][e] += w[S::RA + e + o];
+                        const int off = S::RA + o;
+                        if ((off & 1) == 0) {
+                            acc[r][0] = add_pair<PK>(acc[r][0], make_float2(w[off], w[off + 1]));
+                            acc[r][1] = add_pair<PK>(acc[r][1], make_float2(w[off + 2], w[off + 3]));
+                        } else {
+                            acc[r][0].x += w[off]; acc[r][0].y += w[off + 1];
+                            acc[r][1].x += w[off + 2]; acc[r][1].y += w[off + 3];
+                        }
                     }
                     // axis j
 #pragma unroll
                     for (int o = -R; o <= R; ++o) {
                         if (o == 0) continue;
                         const float4 v = col[r + R + o];
-                        acc[r][0] += v.x; acc[r][1] += v.y; acc[r][2] += v.z; acc[r][3] += v.w;
+                        acc[r][0] = add_pair<PK>(acc[r][0], make_float2(v.x, v.y));
+                        acc[r][1] = add_pair<PK>(acc[r][1], make_float2(v.z, v.w));
                     }
                     // axis k, previous planes z-R .. z-1 (queue indices (ph + R + o) % QN)
 #pragma unroll
                     for (int o = -R; o <= -1; ++o) {
                         const float4 v = qz[r][(ph + R + o + QN) % QN];
-                        acc[r][0] += v.x; acc[r][1] += v.y; acc[r][2] += v.z; acc[r][3] += v.w;
+                        acc[r][0] = add_pair<PK>(acc[r][0], make_float2(v.x, v.y));
+                        acc[r][1] = add_pair<PK>(acc[r][1], make_float2(v.z, v.w));
                     }
                 }
                 // The centre slot is no longer read by this warp.
@@ -190,7 +242,7 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
                     const int pn = step + 2 * R;
                     const uint32_t q = qb + pn;
                     const int s = q & (NS - 1);
-                    if (!mbar_wait_bounded(&full[s], (q / NS) & 1)) return;
+                    if (!mbar_wait_bounded(&full[s], (q / NS) & 1)) { ok = false; break; }
                     const float *sl = ring_own + s * S::SLOT_FLOATS;
 #pragma unroll
                     for (int r = 0; r < RY; ++r) qz[r][(ph + 2 * R) % QN] = lds4(sl + r * S::PW);
@@ -202,7 +254,8 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
 #pragma unroll
                     for (int o = 1; o <= R; ++o) {
                         const float4 v = qz[r][(ph + R + o) % QN];
-                        acc[r][0] += v.x; acc[r][1] += v.y; acc[r][2] += v.z; acc[r][3] += v.w;
+                        acc[r][0] = add_pair<PK>(acc[r][0], make_float2(v.x, v.y));
+                        acc[r][1] = add_pair<PK>(acc[r][1], make_float2(v.z, v.w));
                     }
                 // Epilogue: correctly rounded division by 6R.  The fast path
                 // applies when every stored sum lies in [2^-100, 2^120] (NaN
@@ -212,73 +265,125 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, (R <=
                 for (int r = 0; r < RY; ++r)
                     if (live & (1u << r))
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            lo = fminf(lo, fabsf(acc[r][e]));
-                            hi = fmaxf(hi, fabsf(acc[r][e]));
+                        for (int h = 0; h < 2; ++h) {
+                            lo = fminf(lo, fminf(fabsf(acc[r][h].x), fabsf(acc[r][h].y)));
+                            hi = fmaxf(hi, fmaxf(fabsf(acc[r][h].x), fabsf(acc[r][h].y)));
                         }
                 if (__all_sync(0xffffffffu, lo >= 0x1p-100f && hi <= 0x1p+120f)) {
 #pragma unroll
                     for (int r = 0; r < RY; ++r)
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) acc[r][e] = div_fast<C>(acc[r][e]);
+                        for (int h = 0; h < 2; ++h) acc[r][h] = div_pair<PK, C>(acc[r][h]);
                 } else {
 #pragma unroll
                     for (int r = 0; r < RY; ++r)
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) acc[r][e] = acc[r][e] / (float)C;
+                        for (int h = 0; h < 2; ++h) {
+                            acc[r][h].x = div_slow_from_first<C>(acc[r][h].x);
+                            acc[r][h].y = div_slow_from_first<C>(acc[r][h].y);
+                        }
                 }
                 if (g.legacy) {
 #pragma unroll
                     for (int r = 0; r < RY; ++r) {
                         const float4 c = col[r + R];
-                        acc[r][0] -= c.x; acc[r][1] -= c.y; acc[r][2] -= c.z; acc[r][3] -= c.w;
+                        acc[r][0].x -= c.x; acc[r][0].y -= c.y; acc[r][1].x -= c.z; acc[r][1].y -= c.w;
                     }
                 }
                 if (xin) {
 #pragma unroll
                     for (int r = 0; r < RY; ++r)
                         if (live & (1u << r))
-                            stg4(drow + r * g.sy, acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
+                            stg4(drow + r * g.sy, acc[r][0].x, acc[r][0].y, acc[r][1].x, acc[r][1].y);
                 } else {
 #pragma unroll
                     for (int r = 0; r < RY; ++r)
-                        if (live & (1u << r))
+                        if (live & (1u << r)) {
+                            const float v[4] = {acc[r][0].x, acc[r][0].y, acc[r][1].x, acc[r][1].y};
 #pragma unroll
                             for (int e = 0; e < 4; ++e)
-                                if (in_range(x + e, g.nx, R)) drow[r * g.sy + e] = acc[r][e];
+                                if (in_range(x + e, g.nx, R)) drow[r * g.sy + e] = v[e];
+                        }
                 }
                 drow += g.sz;
             }
         }
         qb += np;
     }
+    if (MULTI && sw + 1 < sweeps) {
+        // Every consumer warp of this CTA has stored its part of sweep sw (or
+        // given up): all of them agree before one thread arrives.
+        ok = named_barrier_and(1, S::CONSUMERS, ok);
+        if (ok && tid == 0) grid_arrive(grid_bar);
+    }
+    }
 }
 
 namespace {
 
 struct StreamKernel {
-    const void *fn;
+    const void *fn;     // one sweep per launch
+    const void *multi;  // persistent: all sweeps in one cooperative launch (default shapes only)
     int tx, ty, threads, smem;
 };
 
-template <int R, int TX, int TY, int RY, int NS>
+template <int R, int TX, int TY, int RY, int NS, bool WITH_MULTI = false>
 StreamKernel sk() {
     using S = StreamShape<R, TX, TY, RY, NS>;
-    return {reinterpret_cast<const void *>(k_stream3d<R, TX, TY, RY, NS>), TX, TY, S::THREADS,
-            S::SMEM_BYTES};
+    const void *multi = nullptr;
+    if constexpr (WITH_MULTI) multi = reinterpret_cast<const void *>(k_stream3d<R, TX, TY, RY, NS, true>);
+    return {reinterpret_cast<const void *>(k_stream3d<R, TX, TY, RY, NS, false>), multi, TX, TY,
+            S::THREADS, S::SMEM_BYTES};
 }
 
 // shape: 0 = 128 x 16, 2 rows per thread; 1 = tall (64 x 32); 2 = one row
 // per thread (more warps, fewer registers each); 3 = a 16-slot ring (more
-// planes in flight, one CTA per SM)
+// planes in flight, one CTA per SM); 4 (R >= 3) = 128 x 16, one row per
+// thread, 16 consumer warps in one CTA; 5 (R <= 2) = 128 x 32, two rows per
+// thread (half the y-halo rows per output row).  The default shape of each
+// radius also has the persistent form.
 StreamKernel pick(int r, int shape) {
     switch (r) {
-        case 1: return shape == 3 ? sk<1, 128, 16, 1, 16>() : shape == 2 ? sk<1, 128, 16, 1, 8>() : shape == 1 ? sk<1, 64, 32, 2, 8>() : sk<1, 128, 16, 2, 8>();
-        case 2: return shape == 3 ? sk<2, 128, 16, 1, 16>() : shape == 2 ? sk<2, 128, 16, 1, 8>() : shape == 1 ? sk<2, 64, 32, 2, 8>() : sk<2, 128, 16, 2, 8>();
-        case 3: return shape == 1 ? sk<3, 64, 32, 2, 8>() : sk<3, 128, 16, 2, 8>();
-        case 4: return shape == 3 ? sk<4, 128, 16, 2, 16>() : shape == 2 ? sk<4, 128, 8, 1, 8>() : shape == 1 ? sk<4, 64, 32, 2, 8>() : sk<4, 128, 16, 2, 8>();
-        default: return {nullptr, 0, 0, 0, 0};
+        case 1: return shape == 5 ? sk<1, 128, 32, 2, 8>() : shape == 3 ? sk<1, 128, 16, 1, 16, true>() : shape == 2 ? sk<1, 128, 16, 1, 8>() : shape == 1 ? sk<1, 64, 32, 2, 8>() : sk<1, 128, 16, 2, 8>();
+        case 2: return shape == 5 ? sk<2, 128, 32, 2, 8, true>() : shape == 3 ? sk<2, 128, 16, 1, 16>() : shape == 2 ? sk<2, 128, 16, 1, 8>() : shape == 1 ? sk<2, 64, 32, 2, 8>() : sk<2, 128, 16, 2, 8>();
+        case 3: return shape == 4 ? sk<3, 128, 16, 1, 8, true>() : shape == 2 ? sk<3, 128, 8, 1, 8>() : shape == 1 ? sk<3, 64, 32, 2, 8>() : sk<3, 128, 16, 2, 8>();
+        case 4: return shape == 4 ? sk<4, 128, 16, 1, 8, true>() : shape == 3 ? sk<4, 128, 16, 2, 16>() : shape == 2 ? sk<4, 128, 8, 1, 8>() : shape == 1 ? sk<4, 64, 32, 2, 8>() : sk<4, 128, 16, 2, 8>();
+        default: return {nullptr, nullptr, 0, 0, 0, 0};
     }
+}
+
+// Grid-barrier counters of the persistent launches: a fixed device array (no
+// allocation, so a launch can be captured in a CUDA graph), one slot per
+// launch taken round-robin and zeroed on the launch's stream just before it.
+constexpr int kGridBarSlots = 256;
+__device__ unsigned g_grid_bar[kGridBarSlots];
+
+int grid_bar_slot(cudaStream_t s, unsigned **slot) {
+    static std::atomic<unsigned> next{0};
+    unsigned *base = nullptr;
+    ST_CUDA(cudaGetSymbolAddress(reinterpret_cast<void **>(&base), g_grid_bar));
+    *slot = base + (next.fetch_add(1) % kGridBarSlots);
+    ST_CUDA(cudaMemsetAsync(*slot, 0, sizeof(unsigned), s));
+    return STENCIL_OK;
+}
+
+// Sets the kernel's shared-memory limit and returns its resident CTAs per SM,
+// once per kernel and device (later calls, e.g. inside a CUDA graph capture,
+// only read the cache).
+int kernel_residency(const void *fn, int threads, int smem, int *per_sm) {
+    static std::mutex mu;
+    static std::vector<std::pair<std::pair<const void *, int>, int>> cache;
+    int dev = 0;
+    ST_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    for (auto &c : cache)
+        if (c.first.first == fn && c.first.second == dev) { *per_sm = c.second; return STENCIL_OK; }
+    ST_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int n = 0;
+    ST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem));
+    cache.push_back({{fn, dev}, n});
+    *per_sm = n;
+    return STENCIL_OK;
 }
 
 }  // namespace
@@ -288,20 +393,25 @@ bool stream3d_supported(const Geom &g) {
 }
 
 int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int tile_y,
-                 cudaStream_t s, float **res, int shape_hint) {
+                 cudaStream_t s, float **res, int shape_hint, bool persistent) {
     const int R = g.radius;
     // Defaults measured fastest at 512^3 on GB300: R = 1 the 16-slot ring
-    // (707 GCell/s vs 615 with 8 slots), R = 2 one row per thread (609 vs 540),
-    // otherwise two rows per thread with an 8-slot ring.
-    int shape = (!tile_x && !tile_y) ? (R == 1 ? 3 : (R == 2 ? 2 : 0))
+    // (707 GCell/s vs 615 with 8 slots), R = 2 128 x 32 tiles (709 vs 609 with
+    // 128 x 16), R >= 3 one row per thread in 16 warps (R = 3: 516 vs 423
+    // with two rows per thread; R = 4: 411 vs 403, before the packed sums).
+    int shape = (!tile_x && !tile_y) ? (R == 1 ? 3 : (R == 2 ? 5 : 4))
                                      : (tile_y == 1 ? 2 : ((tile_x && tile_x < 128) || tile_y > 16 ? 1 : 0));
-    if (shape_hint >= 1 && shape_hint <= 3) shape = shape_hint;
+    if (shape_hint >= 1 && shape_hint <= 5) shape = shape_hint;
+    if (persistent && !(shape_hint >= 1 && shape_hint <= 5)) shape = R == 1 ? 3 : (R == 2 ? 5 : 4);
     StreamKernel k = pick(R, shape);
     if (!k.fn) return fail(STENCIL_EUNSUPPORTED, "stream kernel has no radius-%d instance", R);
+    if (persistent && !k.multi)
+        return fail(STENCIL_EUNSUPPORTED, "the persistent stream kernel exists for the default shapes only");
     if (g.nx % 4) return fail(STENCIL_EUNSUPPORTED, "stream kernel needs nx %% 4 == 0");
-    ST_CUDA(cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, k.smem));
+    const void *fn = persistent ? k.multi : k.fn;
     int per_sm = 0;
-    ST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, k.threads, k.smem));
+    int rc = kernel_residency(fn, k.threads, k.smem, &per_sm);
+    if (rc) return rc;
     if (per_sm < 1) return fail(STENCIL_EUNSUPPORTED, "stream kernel does not fit on an SM");
     const int resident = per_sm * num_sms();
     const int tiles_x = (g.nx + k.tx - 1) / k.tx, tiles_y = (g.ny + k.ty - 1) / k.ty;
@@ -331,16 +441,35 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     CUtensorMap maps[2];
     const long long dims[3] = {g.nx, g.ny, g.nz};
     const int box[3] = {k.tx + 2 * ((R + 3) & ~3), k.ty + 2 * R, 1};
-    int rc = make_tensor_map(&maps[0], a, 3, dims, box);
+    rc = make_tensor_map(&maps[0], a, 3, dims, box);
     if (!rc) rc = make_tensor_map(&maps[1], b, 3, dims, box);
     if (rc) return rc;
-    float *cur = a, *nxt = b;
-    int ci = 0;
     Geom gg = g;
     int tx_ = tiles_x, ty_ = tiles_y, it_ = items;
+    if (persistent) {
+        // One cooperative launch (every CTA resident, as the grid barrier
+        // needs): sweep k reads maps[k & 1] and writes the other buffer.
+        if (iters > 0) {
+            unsigned *bar = nullptr;
+            rc = grid_bar_slot(s, &bar);
+            if (rc) return rc;
+            float *d0 = b, *d1 = a;
+            int sw = iters;
+            void *args[] = {&maps[0], &maps[1], &d0, &d1, &gg, &tx_, &ty_, &zchunk, &it_, &sw, &bar};
+            ST_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(k.threads), args, k.smem, s));
+            note_launches("stream3d-persistent", 1);
+        }
+        if (res) *res = (iters & 1) ? b : a;
+        return STENCIL_OK;
+    }
+    note_launches("stream3d", iters);
+    float *cur = a, *nxt = b;
+    int ci = 0;
+    int one = 1;
+    unsigned *no_bar = nullptr;
     for (int it = 0; it < iters; ++it) {
-        void *args[] = {&maps[ci], &nxt, &gg, &tx_, &ty_, &zchunk, &it_};
-        ST_CUDA(cudaLaunchKernel(k.fn, dim3(grid), dim3(k.threads), args, k.smem, s));
+        void *args[] = {&maps[ci], &maps[ci], &nxt, &nxt, &gg, &tx_, &ty_, &zchunk, &it_, &one, &no_bar};
+        ST_CUDA(cudaLaunchKernel(fn, dim3(grid), dim3(k.threads), args, k.smem, s));
         std::swap(cur, nxt);
         ci ^= 1;
     }

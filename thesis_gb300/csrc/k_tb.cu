@@ -352,6 +352,7 @@ int run_tb3d(const Geom &g, float *a, float *b, int iters, int temporal, cudaStr
     int tx_ = tiles_x;
     long long tot_ = total;
     const int passes = iters / k.T;
+    note_launches("tb3d", passes);
     for (int it = 0; it < passes; ++it) {
         void *args[] = {&maps[ci], &nxt, &gg, &tx_, &tot_};
         ST_CUDA(cudaLaunchKernel(k.fn, dim3(grid), dim3(k.threads), args, k.smem, s));

@@ -65,7 +65,8 @@ constexpr int BM = 128, BK = 32, PITCH = BK + 8;  // 80-byte rows: conflict-free
 
 template <int BN>
 __global__ void __launch_bounds__(128)
-    k_conv3x3(Act x, const bf16 *__restrict__ w, const float *__restrict__ bias, Act y, int relu) {
+    k_conv3x3(Act x, const bf16 *__restrict__ w, const float *__restrict__ bias, Act y, int relu,
+              int dil) {
     __shared__ __align__(128) bf16 As[2][BM][PITCH];
     __shared__ __align__(128) bf16 Bs[2][BN][PITCH];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -90,7 +91,7 @@ __global__ void __launch_bounds__(128)
     }
     auto load = [&](int kb, int st) {
         const int tap = kb / nc, c0 = (kb % nc) * BK;
-        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+        const int dy = (tap / 3 - 1) * dil, dx = (tap % 3 - 1) * dil;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int idx = tid + 128 * i, row = idx >> 2, part = idx & 3;
@@ -174,14 +175,14 @@ __global__ void __launch_bounds__(128)
 constexpr int WK = 32, WPITCH = 64 + 8;
 
 __global__ void __launch_bounds__(128)
-    k_wgrad(Act x, Act dy, float *__restrict__ dw, long long pix_per_block) {
+    k_wgrad(Act x, Act dy, float *__restrict__ dw, long long pix_per_block, int dil) {
     __shared__ __align__(128) bf16 As[2][WK][WPITCH];  // [p][co]
     __shared__ __align__(128) bf16 Bs[2][WK][WPITCH];  // [p][ci]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int wm = warp & 1, wn = warp >> 1;
     const int co0 = blockIdx.x * 64, ci0 = blockIdx.y * 64;
     const int tap = blockIdx.z % 9, split = blockIdx.z / 9;
-    const int ddy = tap / 3 - 1, ddx = tap % 3 - 1;
+    const int ddy = (tap / 3 - 1) * dil, ddx = (tap % 3 - 1) * dil;
     const long long P = (long long)x.n * x.h * x.w;
     const long long pb = split * pix_per_block, pe = min(P, pb + pix_per_block);
     if (pb >= pe) return;
@@ -615,11 +616,12 @@ using namespace st;
     do { int rc_ = check_act(v, #v); if (rc_) return rc_; } while (0)
 #define STREAM(s) reinterpret_cast<cudaStream_t>(s)
 
-extern "C" int unet_conv3x3_fwd(const unet_act *x, const void *w, const float *b, const unet_act *y,
-                                int relu, stencil_stream_t s) {
+extern "C" int unet_conv3x3_fwd_dil(const unet_act *x, const void *w, const float *b,
+                                    const unet_act *y, int relu, int dilation, stencil_stream_t s) {
     CHECK_VIEW(x);
     CHECK_VIEW(y);
     if (!w) return fail(STENCIL_EINVAL, "null weights");
+    if (dilation < 1) return fail(STENCIL_EINVAL, "dilation must be >= 1");
     if (x->c % 32 || y->c % 32) return fail(STENCIL_EINVAL, "channels must be multiples of 32");
     if (x->n != y->n || x->h != y->h || x->w != y->w) return fail(STENCIL_EINVAL, "shape mismatch");
     const long long P = (long long)x->n * x->h * x->w;
@@ -627,12 +629,17 @@ extern "C" int unet_conv3x3_fwd(const unet_act *x, const void *w, const float *b
     const bf16 *wb = static_cast<const bf16 *>(w);
     if (y->c % 64 == 0) {
         dim3 grid((unsigned)((P + BM - 1) / BM), y->c / 64);
-        k_conv3x3<64><<<grid, 128, 0, STREAM(s)>>>(xa, wb, b, ya, relu);
+        k_conv3x3<64><<<grid, 128, 0, STREAM(s)>>>(xa, wb, b, ya, relu, dilation);
     } else {
         dim3 grid((unsigned)((P + BM - 1) / BM), y->c / 32);
-        k_conv3x3<32><<<grid, 128, 0, STREAM(s)>>>(xa, wb, b, ya, relu);
+        k_conv3x3<32><<<grid, 128, 0, STREAM(s)>>>(xa, wb, b, ya, relu, dilation);
     }
     return cuda_fail(cudaGetLastError(), "conv3x3 launch");
+}
+
+extern "C" int unet_conv3x3_fwd(const unet_act *x, const void *w, const float *b, const unet_act *y,
+                                int relu, stencil_stream_t s) {
+    return unet_conv3x3_fwd_dil(x, w, b, y, relu, 1, s);
 }
 
 extern "C" int unet_flip_weights(const void *w, void *wt, int cout, int cin, stencil_stream_t s) {
@@ -642,11 +649,12 @@ extern "C" int unet_flip_weights(const void *w, void *wt, int cout, int cin, ste
     return cuda_fail(cudaGetLastError(), "flip launch");
 }
 
-extern "C" int unet_conv3x3_wgrad(const unet_act *x, const unet_act *dy, float *dw, float *db,
-                                  stencil_stream_t s) {
+extern "C" int unet_conv3x3_wgrad_dil(const unet_act *x, const unet_act *dy, float *dw, float *db,
+                                      int dilation, stencil_stream_t s) {
     CHECK_VIEW(x);
     CHECK_VIEW(dy);
     if (!dw) return fail(STENCIL_EINVAL, "null dw");
+    if (dilation < 1) return fail(STENCIL_EINVAL, "dilation must be >= 1");
     if (x->n != dy->n || x->h != dy->h || x->w != dy->w) return fail(STENCIL_EINVAL, "shape mismatch");
     const long long P = (long long)x->n * x->h * x->w;
     const int mt = (dy->c + 63) / 64, nt = (x->c + 63) / 64;
@@ -657,12 +665,17 @@ extern "C" int unet_conv3x3_wgrad(const unet_act *x, const unet_act *dy, float *
     per = ((per + WK - 1) / WK) * WK;
     splits = (P + per - 1) / per;
     dim3 grid(mt, nt, (unsigned)(9 * splits));
-    k_wgrad<<<grid, 128, 0, STREAM(s)>>>(to_act(*x), to_act(*dy), dw, per);
+    k_wgrad<<<grid, 128, 0, STREAM(s)>>>(to_act(*x), to_act(*dy), dw, per, dilation);
     int rc = cuda_fail(cudaGetLastError(), "wgrad launch");
     if (rc || !db) return rc;
     dim3 g2((unsigned)std::min<long long>(1024, (P + 255) / 256), (dy->c + 31) / 32);
     k_bias_grad<<<g2, 256, 0, STREAM(s)>>>(to_act(*dy), db);
     return cuda_fail(cudaGetLastError(), "bias grad launch");
+}
+
+extern "C" int unet_conv3x3_wgrad(const unet_act *x, const unet_act *dy, float *dw, float *db,
+                                  stencil_stream_t s) {
+    return unet_conv3x3_wgrad_dil(x, dy, dw, db, 1, s);
 }
 
 extern "C" int unet_relu_bwd(const unet_act *g, const unet_act *y, stencil_stream_t s) {

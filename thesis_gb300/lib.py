@@ -85,6 +85,11 @@ def load() -> ctypes.CDLL:
         "stencil_params_check": (i, [P]),
         "stencil_dispatch_ex": (i, [P, vp, vp, vp, ctypes.POINTER(vp)]),
         "stencil_run_host": (i, [P, vp, vp, ctypes.POINTER(ctypes.c_float)]),
+        "stencil_last_dispatch": (i, [ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_longlong)]),
+        "stencil_heuristic_block": (i, [P, i, ctypes.POINTER(i), ctypes.POINTER(i),
+                                        ctypes.POINTER(i)]),
+        "stencil_run_host_timed": (i, [P, vp, vp, ctypes.POINTER(ctypes.c_float),
+                                       ctypes.POINTER(ctypes.c_float)]),
         "stencil_init_reference": (i, [P, vp, vp]),
         "stencil_init_uniform": (i, [vp, sz, u64, vp]),
         "stencil_copy_border": (i, [P, vp, vp, vp]),

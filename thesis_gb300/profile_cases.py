@@ -15,9 +15,10 @@ def main(case):
     from . import build, lib, stencil as S
     build.build()
     J = lib.MODE_JACOBI
-    if case in ("stream_r1", "stream_r4"):
-        R = 1 if case == "stream_r1" else 4
-        u = S.init_uniform((320, 320, 320), 1)  # 131 MB per buffer
+    if case in ("stream_r1", "stream_r4", "stream_r1_512", "stream_r4_512"):
+        R = 1 if case.startswith("stream_r1") else 4
+        n = 512 if case.endswith("_512") else 320
+        u = S.init_uniform((n, n, n), 1)  # 131 MB (320^3) or 537 MB (512^3) per buffer
         a, b = u.clone(), u.clone()
         for _ in range(4):
             S.sweep(a, b, R, 2, J, "smem_register")

@@ -161,18 +161,30 @@ def residual(u, radius: int, stream=None) -> float:
 
 def run_host(h_in: np.ndarray, radius: int, iterations: int, mode: int = _lib.MODE_JACOBI,
              variant="auto", block=(0, 0, 0), coarsen_x: int = 0, temporal: int = 0,
-             out: np.ndarray | None = None):
-    """End to end from host memory (stencil_run_host); returns (result, ms)."""
+             out: np.ndarray | None = None, sweeps_ms: bool = False):
+    """End to end from host memory (stencil_run_host_timed); returns (result,
+    ms) with ms the upload + sweeps + download time, or (result, ms, ms_sweeps)
+    when sweeps_ms is set (ms_sweeps = the sweeps alone, the figure the
+    reference's binary prints)."""
     h_in = np.ascontiguousarray(h_in, dtype=np.float32)
     if out is None:
         out = np.empty_like(h_in)
     p = _lib.make_params(h_in.shape, radius, iterations, mode, variant, block, coarsen_x,
                          temporal)
-    ms = ctypes.c_float()
-    _lib.check(_lib.load().stencil_run_host(ctypes.byref(p), ctypes.c_void_p(h_in.ctypes.data),
-                                            ctypes.c_void_p(out.ctypes.data), ctypes.byref(ms)),
-               "stencil_run_host")
-    return out, ms.value
+    ms, ms_sw = ctypes.c_float(), ctypes.c_float()
+    _lib.check(_lib.load().stencil_run_host_timed(ctypes.byref(p), ctypes.c_void_p(h_in.ctypes.data),
+                                                  ctypes.c_void_p(out.ctypes.data), ctypes.byref(ms),
+                                                  ctypes.byref(ms_sw)),
+               "stencil_run_host_timed")
+    return (out, ms.value, ms_sw.value) if sweeps_ms else (out, ms.value)
+
+
+def last_dispatch():
+    """(engine, kernel launches) of this thread's last dispatch."""
+    eng, n = ctypes.c_char_p(), ctypes.c_longlong()
+    _lib.check(_lib.load().stencil_last_dispatch(ctypes.byref(eng), ctypes.byref(n)),
+               "stencil_last_dispatch")
+    return (eng.value or b"").decode(), n.value
 
 
 def device_status() -> int:

@@ -11,6 +11,10 @@ Architecture (4 levels, 32 base channels, 3x3 convolutions, ReLU):
   enc0 32-32 | pool | enc1 64-64 | pool | enc2 128-128 | pool | bottom 256-256
   up + cat(enc2) 384 -> 128-128 | up + cat(enc1) 192 -> 64-64 |
   up + cat(enc0) 96 -> 32-32 | 1x1 head -> 1
+The two bottom convolutions take their taps 2 and 4 cells apart (dilation):
+the receptive field then reaches about 80 cells from each output cell, so at
+the 128 x 128 training size every interior cell sees all four borders (with
+undilated taps it reaches 48, and the centre of the grid sees none).
 Inputs (3 of 32 padded channels): the border field, the border mask and the
 transfinite (Coons) interpolation of the border.  The head predicts the
 correction to the Coons field on interior cells.
@@ -25,6 +29,7 @@ import numpy as np
 from . import lib as _lib
 
 IN_CH = 32
+DILATION = {"ba": 2, "bb": 4}  # layers whose taps are spread (default 1)
 LAYERS = [  # name, cin, cout
     ("e0a", IN_CH, 32), ("e0b", 32, 32),
     ("e1a", 32, 64), ("e1b", 64, 64),
@@ -53,6 +58,8 @@ def _L():
         vp, i, f, ll = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_longlong
         sig = {
             "unet_conv3x3_fwd": [A, vp, vp, A, i, vp],
+            "unet_conv3x3_fwd_dil": [A, vp, vp, A, i, i, vp],
+            "unet_conv3x3_wgrad_dil": [A, A, vp, vp, i, vp],
             "unet_flip_weights": [vp, vp, i, i, vp],
             "unet_conv3x3_wgrad": [A, A, vp, vp, vp],
             "unet_relu_bwd": [A, A, vp],
@@ -203,7 +210,8 @@ class UNet:
     # -- forward -----------------------------------------------------------
     def _conv(self, name, x, y, s):
         P = self.params[name]
-        _chk(_L().unet_conv3x3_fwd(ctypes.byref(x), _p(P["wb"]), _p(P["b"]), ctypes.byref(y), 1, s),
+        _chk(_L().unet_conv3x3_fwd_dil(ctypes.byref(x), _p(P["wb"]), _p(P["b"]), ctypes.byref(y), 1,
+                                       DILATION.get(name, 1), s),
              "conv " + name)
 
     def forward(self, fields, stream=None):
@@ -246,12 +254,13 @@ class UNet:
         L = _L()
         P = self.params[name]
         _chk(L.unet_relu_bwd(ctypes.byref(gy), ctypes.byref(y), s), "relu_bwd " + name)
-        _chk(L.unet_conv3x3_wgrad(ctypes.byref(x), ctypes.byref(gy), _p(P["dw"]), _p(P["db"]), s),
+        d = DILATION.get(name, 1)
+        _chk(L.unet_conv3x3_wgrad_dil(ctypes.byref(x), ctypes.byref(gy), _p(P["dw"]), _p(P["db"]), d, s),
              "wgrad " + name)
         if gx is not None:
             cin, cout = P["w"].shape[2], P["w"].shape[0]
             _chk(L.unet_flip_weights(_p(P["wb"]), _p(P["wt"]), cout, cin, s), "flip " + name)
-            _chk(L.unet_conv3x3_fwd(ctypes.byref(gy), _p(P["wt"]), None, ctypes.byref(gx), 0, s),
+            _chk(L.unet_conv3x3_fwd_dil(ctypes.byref(gy), _p(P["wt"]), None, ctypes.byref(gx), 0, d, s),
                  "dgrad " + name)
 
     def zero_grad(self):

@@ -232,7 +232,8 @@ def main():
     ap.add_argument("--pairs", type=int, default=20000)
     ap.add_argument("--size", type=int, default=128)
     ap.add_argument("--gen-sweeps", type=int, default=40000)
-    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--epochs", type=int, default=40)
+    ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--eval", type=int, default=256)
     ap.add_argument("--eval-size", type=int, default=512)
@@ -249,7 +250,7 @@ def main():
     rres = [S.residual(sols[k], 1) for k in range(0, args.pairs, max(1, args.pairs // 16))]
     print("generated %d pairs in %.1f s, sample residual max %.2e" % (args.pairs, gen_s, max(rres)))
     net = UNet(seed=0)
-    losses, train_s = train(net, fields, sols, args.epochs, args.batch, log=print)
+    losses, train_s = train(net, fields, sols, args.epochs, args.batch, lr=args.lr, log=print)
     print("trained in %.1f s" % train_s)
     if args.save:
         net.save(args.save)
@@ -258,6 +259,7 @@ def main():
     seeds = list(range(10_000_000, 10_000_000 + args.eval))
     res = evaluate(net, seeds, args.eval_size, args.tol)
     res.update({"pairs": args.pairs, "gen_s": gen_s, "train_s": train_s, "epochs": args.epochs,
+                "lr": args.lr,
                 "final_loss": losses[-1] if losses else None})
     print(json.dumps(res))
     if args.json:
