@@ -5,7 +5,11 @@
 * ``build_ref(configs)`` compiles the reference's own ``src/stencil_cpu.cu``
   through the wrapper ``ref_cpu_main.cu`` with nvcc, one binary per
   (DIMENSIONS, DIM, RADIUS, ITERATIONS), into ``oracle/_ref/``.  It needs the
-  reference sources and is skipped where they are absent.  The reference
+  reference sources and is skipped where they are absent.
+* ``build_ref_gpu(configs)`` compiles the reference's own one-sweep GPU
+  kernels through the wrapper ``ref_gpu_kernels.cu`` into one sm_103a cubin
+  per compile-time configuration, into ``oracle/_ref/`` (device code only, so
+  the cubins built here run on the GPU host, which has no reference sources).  The reference
   Makefile's own ``stencil_cpu`` target cannot be used: src/stencil_cpu.cpp:1
   includes a header that does not exist and Makefile:72-73 compiles CUDA code
   with gcc.
@@ -68,6 +72,52 @@ def build_ref(configs, jobs: int = 8) -> list[str]:
     for p in procs:
         if p.wait() != 0:
             raise RuntimeError("reference CPU build failed")
+    return out
+
+
+# Reference GPU kernel configurations: (DIMENSIONS, DIM, RADIUS, BLOCK_X,
+# BLOCK_Y, BLOCK_Z, COARSEN_X).  Every variant is built for each; the DIM 64
+# ones serve the parity tests (golden fixtures), the 512 ones the speed
+# comparison.
+REF_GPU_SHAPES_512 = [(32, 4, 4, 1), (32, 8, 4, 1), (64, 4, 4, 1), (32, 8, 2, 1), (32, 4, 4, 2),
+                      (32, 8, 2, 4)]
+REF_GPU_CONFIGS = ([(3, 64, r, 32, 4, 4, 1) for r in (1, 2)] + [(3, 64, 2, 32, 4, 4, 2)] +
+                   [(3, 512, r, bx, by, bz, cf) for r in (1, 4) for (bx, by, bz, cf) in REF_GPU_SHAPES_512])
+
+
+def ref_cubin(cfg) -> str:
+    return os.path.join(REF_DIR, "gpu_%dd_%d_r%d_b%dx%dx%d_cf%d.cubin" % tuple(cfg))
+
+
+def build_ref_gpu(configs=None, jobs: int = 8) -> list[str]:
+    """One cubin per configuration.  The variant (base, smem, smem_padded,
+    smem_register) is chosen at launch by kernel name, so the SMEM, PADDED and
+    REGISTER macros stay at their defaults here."""
+    if not reference_available():
+        return []
+    os.makedirs(REF_DIR, exist_ok=True)
+    wrapper = os.path.join(HERE, "ref_gpu_kernels.cu")
+    procs, out = [], []
+    for cfg in configs or REF_GPU_CONFIGS:
+        dims, dim, radius, bx, by, bz, cf = cfg
+        cub = ref_cubin(cfg)
+        out.append(cub)
+        if os.path.exists(cub) and os.path.getmtime(cub) >= os.path.getmtime(wrapper):
+            continue
+        cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+               "-I", REF_ROOT, "-o", cub, wrapper,
+               "-D", "DIMENSIONS=%d" % dims, "-D", "DIM=%d" % dim, "-D", "RADIUS=%d" % radius,
+               "-D", "BLOCK_X=%d" % bx, "-D", "BLOCK_Y=%d" % by, "-D", "BLOCK_Z=%d" % bz,
+               "-D", "COARSEN_X=%d" % cf]
+        procs.append(subprocess.Popen(cmd))
+        if len(procs) >= jobs:
+            for p in procs:
+                if p.wait() != 0:
+                    raise RuntimeError("reference GPU kernel build failed")
+            procs = []
+    for p in procs:
+        if p.wait() != 0:
+            raise RuntimeError("reference GPU kernel build failed")
     return out
 
 

@@ -48,7 +48,7 @@ struct StreamShape {
     static constexpr int CONSUMERS = CW * (TY / RY);
     static constexpr int CWARPS = CONSUMERS / 32;
     static constexpr int THREADS = CONSUMERS + 32;
-    static constexpr int SMEM_BYTES = NS * SLOT_FLOATS * 4 + 128 + 2 * NS * 8;
+    static constexpr int SMEM_BYTES = NS * SLOT_FLOATS * 4 + 128 + (2 * NS + 1) * 8;
     // Two resident CTAs where the registers allow: the 8-slot R = 1 shapes
     // of 9 warps, or of 17 one-row warps (56 registers), and the
     // one-row-per-thread 9-warp shapes at larger radii (their budget, 96 to
@@ -88,11 +88,18 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, Strea
     using S = StreamShape<R, TX, TY, RY, NS>;
     constexpr int C = 6 * R;  // 2*D*R with D = 3
     constexpr bool PK = R >= 3;
+    // How a consumer warp leaves after a bounded wait gave up: R = 1 returns
+    // at once; R >= 2 clears `ok` and leaves its loops, and the warps agree at
+    // a named barrier.  Same behaviour, but the code generated for each form
+    // differs in speed (same-box A/B at 512^3: R = 1 713 vs 628 GCell/s with
+    // early returns; R = 4 541 vs 467 with the flag).
+    constexpr bool FLAG_EXIT = R >= 2;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float *ring = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
                                             ~static_cast<uintptr_t>(127));
     uint64_t *full = reinterpret_cast<uint64_t *>(ring + NS * S::SLOT_FLOATS);
     uint64_t *empty = full + NS;
+    uint64_t *swept = empty + NS;  // MULTI, R = 1: every consumer warp has stored its part of a sweep
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (!MULTI) sweeps = 1;
     if (tid == 0) {
@@ -102,6 +109,7 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, Strea
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], S::CWARPS);
         }
+        mbar_init(swept, S::CWARPS);
         fence_mbar_init();
     }
     __syncthreads();
@@ -164,7 +172,9 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, Strea
         for (int p = 0; p < 2 * R; ++p) {
             const uint32_t q = qb + p;
             const int s = q & (NS - 1);
-            if (!mbar_wait_bounded(&full[s], (q / NS) & 1)) { ok = false; break; }
+            if (!mbar_wait_bounded(&full[s], (q / NS) & 1)) {
+                if constexpr (FLAG_EXIT) { ok = false; break; } else { return; }
+            }
             const float *sl = ring + s * S::SLOT_FLOATS + own;
 #pragma unroll
             for (int r = 0; r < RY; ++r) qz[r][p] = lds4(sl + r * S::PW);
@@ -242,7 +252,9 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, Strea
                     const int pn = step + 2 * R;
                     const uint32_t q = qb + pn;
                     const int s = q & (NS - 1);
-                    if (!mbar_wait_bounded(&full[s], (q / NS) & 1)) { ok = false; break; }
+                    if (!mbar_wait_bounded(&full[s], (q / NS) & 1)) {
+                        if constexpr (FLAG_EXIT) { ok = false; break; } else { return; }
+                    }
                     const float *sl = ring_own + s * S::SLOT_FLOATS;
 #pragma unroll
                     for (int r = 0; r < RY; ++r) qz[r][(ph + 2 * R) % QN] = lds4(sl + r * S::PW);
@@ -311,9 +323,16 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, Strea
         qb += np;
     }
     if (MULTI && sw + 1 < sweeps) {
-        // Every consumer warp of this CTA has stored its part of sweep sw (or
-        // given up): all of them agree before one thread arrives.
-        ok = named_barrier_and(1, S::CONSUMERS, ok);
+        // Once every consumer warp of this CTA has stored its part of sweep
+        // sw (or given up), one thread arrives at the grid barrier.
+        if constexpr (FLAG_EXIT) {
+            ok = named_barrier_and(1, S::CONSUMERS, ok);
+        } else {
+            // a warp that gave up has returned; the others give up here
+            __syncwarp();
+            if (lane == 0) mbar_arrive(swept);
+            if (!mbar_wait_bounded(swept, sw & 1)) return;
+        }
         if (ok && tid == 0) grid_arrive(grid_bar);
     }
     }

@@ -22,6 +22,13 @@ def main(case):
         a, b = u.clone(), u.clone()
         for _ in range(4):
             S.sweep(a, b, R, 2, J, "smem_register")
+    elif case in ("persist_r1_512", "persist_r4_512"):
+        # the persistent engine AUTO runs: 8 sweeps in one cooperative launch
+        R = 1 if case == "persist_r1_512" else 4
+        u = S.init_uniform((512, 512, 512), 1)
+        a, b = u.clone(), u.clone()
+        for _ in range(3):
+            S.sweep(a, b, R, 8, J, "coop", temporal=1)
     elif case in ("tb_r1_t2", "tb_r1_t4"):
         T = 2 if case.endswith("t2") else 4
         u = S.init_uniform((320, 320, 320), 1)
