@@ -100,8 +100,8 @@ static EncodeTiledFn encode_fn() {
     return fn;
 }
 
-int make_tensor_map(CUtensorMap *map, const float *base, int rank, const long long *dims,
-                    const int *box) {
+int make_tensor_map_typed(CUtensorMap *map, const void *base, int rank, const long long *dims,
+                          const int *box, CUtensorMapDataType dtype, int elem_bytes) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return fail(STENCIL_ECUDA, "cuTensorMapEncodeTiled is unavailable");
     cuuint64_t gdim[3], gstride[2];
@@ -110,14 +110,18 @@ int make_tensor_map(CUtensorMap *map, const float *base, int rank, const long lo
         gdim[i] = (cuuint64_t)dims[i];
         bdim[i] = (cuuint32_t)box[i];
     }
-    gstride[0] = (cuuint64_t)dims[0] * 4;
-    if (rank == 3) gstride[1] = (cuuint64_t)dims[0] * dims[1] * 4;
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank,
-                    const_cast<float *>(base), gdim, gstride, bdim, estride,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+    gstride[0] = (cuuint64_t)dims[0] * elem_bytes;
+    if (rank == 3) gstride[1] = (cuuint64_t)dims[0] * dims[1] * elem_bytes;
+    CUresult r = fn(map, dtype, (cuuint32_t)rank, const_cast<void *>(base), gdim, gstride, bdim,
+                    estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(STENCIL_EINVAL, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return STENCIL_OK;
+}
+
+int make_tensor_map(CUtensorMap *map, const float *base, int rank, const long long *dims,
+                    const int *box) {
+    return make_tensor_map_typed(map, base, rank, dims, box, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4);
 }
 
 // Per-device scratch kept between calls (host-buffer entry, residual).

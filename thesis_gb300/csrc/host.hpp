@@ -30,6 +30,9 @@ int current_device();
 // Builds a tiled TMA descriptor for an FP32 grid (rank 2 or 3).
 int make_tensor_map(CUtensorMap *map, const float *base, int rank, const long long *dims,
                     const int *box);
+// The same for another element type (e.g. BF16/FP16 grids, 2 bytes).
+int make_tensor_map_typed(CUtensorMap *map, const void *base, int rank, const long long *dims,
+                          const int *box, CUtensorMapDataType dtype, int elem_bytes);
 
 // One sweep per launch kernels (src -> dst).  Each returns a status.
 int launch_base_sweep(const Geom &g, int dims, const float *src, float *dst, int bx, int by,

@@ -13,7 +13,8 @@
 // total sweep count means the same as for the FP32 loop; only rounding
 // differs.  The FP64 relative residual (k_util.cu) decides convergence when a
 // tolerance is given.  Correction sweeps move 6 bytes per cell update (read e
-// and r, write e) instead of 8.
+// and r, write e) instead of 8; on 3-D grids they run on the TMA-fed stream
+// form (k_lpstream.cu), elsewhere on k_lp_sweep below (the same arithmetic).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -25,6 +26,10 @@ namespace st {
 
 size_t residual_scratch_bytes();
 int launch_residual(const Geom &g, int dims, const float *u, double *scratch, cudaStream_t s);
+// The TMA-fed correction sweep for 3-D grids (k_lpstream.cu).
+bool lp_stream_supported(const Geom &g, int dims);
+template <typename E>
+int launch_lp_stream(const Geom &g, const E *e, E *eo, const E *rhs, cudaStream_t s);
 
 template <typename E>
 struct LowP;
@@ -226,8 +231,14 @@ int ir_loop(const stencil_params &p, const stencil_ir_params &ir, float *u, char
         ST_CUDA(cudaGetLastError());
         ST_CUDA(cudaMemcpyAsync(ea, r, n * sizeof(E), cudaMemcpyDeviceToDevice, s));
         E *cur = ea, *nxt = eb;
+        const bool streamed = lp_stream_supported(g, D);
         for (int it = 1; it < m; ++it) {
-            k_lp_sweep<E, D, R><<<8 * num_sms(), 256, 0, s>>>(cur, nxt, r, g);
+            if (streamed) {
+                int rc = launch_lp_stream<E>(g, cur, nxt, r, s);
+                if (rc) return rc;
+            } else {
+                k_lp_sweep<E, D, R><<<8 * num_sms(), 256, 0, s>>>(cur, nxt, r, g);
+            }
             std::swap(cur, nxt);
         }
         ST_CUDA(cudaGetLastError());
