@@ -8,8 +8,10 @@
 //   * a consumer thread owns 4 consecutive cells of one row: it converts the
 //     z-neighbours once, when their plane arrives, into an FP32 register queue
 //     of 2R+1 planes; x- and y-neighbours come from the centre slot as 8-byte
-//     loads converted on use; its rhs values come from global memory one
-//     plane ahead;
+//     loads and enter the FP32 sums through mixed-precision adds
+//     (add.rn.f32.bf16 / .f16: the 16-bit operand is converted exactly, one
+//     rounding, no separate conversion); its rhs values come from global
+//     memory one plane ahead;
 //   * the sum runs in the order of the FP32 sweep (axis i, j, k; offsets -R..-1,
 //     +1..+R), starts from its first term, and is divided as there, then rhs
 //     is added, so each cell equals the cell-by-cell correction sweep
@@ -39,6 +41,17 @@ struct Cvt<__nv_bfloat16> {
         __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
         return *reinterpret_cast<uint32_t *>(&h);
     }
+    // acc + (half H of w), one rounding: the mixed-precision add converts the
+    // BF16 operand exactly, so this equals acc + (float)value
+    template <int H>
+    __device__ static float add(uint32_t w, float acc) {
+        float d;
+        if constexpr (H == 0)
+            asm("{.reg .b16 l, h; mov.b32 {l, h}, %1; add.rn.f32.bf16 %0, l, %2;}" : "=f"(d) : "r"(w), "f"(acc));
+        else
+            asm("{.reg .b16 l, h; mov.b32 {l, h}, %1; add.rn.f32.bf16 %0, h, %2;}" : "=f"(d) : "r"(w), "f"(acc));
+        return d;
+    }
     static constexpr CUtensorMapDataType kTma = CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
 };
 template <>
@@ -50,13 +63,78 @@ struct Cvt<__half> {
         __half2 h = __floats2half2_rn(a, b);
         return *reinterpret_cast<uint32_t *>(&h);
     }
+    template <int H>
+    __device__ static float add(uint32_t w, float acc) {
+        float d;
+        if constexpr (H == 0)
+            asm("{.reg .b16 l, h; mov.b32 {l, h}, %1; add.rn.f32.f16 %0, l, %2;}" : "=f"(d) : "r"(w), "f"(acc));
+        else
+            asm("{.reg .b16 l, h; mov.b32 {l, h}, %1; add.rn.f32.f16 %0, h, %2;}" : "=f"(d) : "r"(w), "f"(acc));
+        return d;
+    }
     static constexpr CUtensorMapDataType kTma = CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
 };
+
+// acc + value of cell c (0 .. 11) of the 6 words holding cells x-4 .. x+7
+template <typename E, int CELL>
+__device__ __forceinline__ float add_cell(const uint32_t (&wd)[6], float acc) {
+    return Cvt<E>::template add<CELL & 1>(wd[CELL >> 1], acc);
+}
+
+// the four cells of one 8-byte row segment added to four sums
+template <typename E>
+__device__ __forceinline__ void add_row(uint2 v, float (&acc)[4]) {
+    acc[0] = Cvt<E>::template add<0>(v.x, acc[0]);
+    acc[1] = Cvt<E>::template add<1>(v.x, acc[1]);
+    acc[2] = Cvt<E>::template add<0>(v.y, acc[2]);
+    acc[3] = Cvt<E>::template add<1>(v.y, acc[3]);
+}
+
+template <int E0, int O, int R, typename E>
+__device__ __forceinline__ void add_x(const uint32_t (&wd)[6], float (&acc)[4]) {
+    acc[E0] = add_cell<E, 4 + E0 + O>(wd, acc[E0]);
+}
 
 template <typename E>
 __device__ __forceinline__ float4 to4(uint2 v) {
     const float2 a = Cvt<E>::two(v.x), b = Cvt<E>::two(v.y);
     return make_float4(a.x, a.y, b.x, b.y);
+}
+
+// axis-i sum of the four cells in the reference order (offsets -R..-1, +1..+R)
+template <typename E, int R, int O = -R>
+__device__ __forceinline__ void xsum(const uint32_t (&wd)[6], float (&acc)[4]) {
+    if constexpr (O == -R) {
+        acc[0] = add_cell<E, 4 + 0 + O>(wd, -0.0f);
+        acc[1] = add_cell<E, 4 + 1 + O>(wd, -0.0f);
+        acc[2] = add_cell<E, 4 + 2 + O>(wd, -0.0f);
+        acc[3] = add_cell<E, 4 + 3 + O>(wd, -0.0f);
+    } else if constexpr (O != 0) {
+        acc[0] = add_cell<E, 4 + 0 + O>(wd, acc[0]);
+        acc[1] = add_cell<E, 4 + 1 + O>(wd, acc[1]);
+        acc[2] = add_cell<E, 4 + 2 + O>(wd, acc[2]);
+        acc[3] = add_cell<E, 4 + 3 + O>(wd, acc[3]);
+    }
+    if constexpr (O < R) xsum<E, R, O + 1>(wd, acc);
+}
+
+// four FP32 queue values added to four sums (as pairs where the kernel is
+// issue-bound, R >= 3; the same roundings either way)
+template <bool PK>
+__device__ __forceinline__ void add_q(float4 v, float (&acc)[4]) {
+    if constexpr (PK) {
+        const float2 a = fadd2(make_float2(acc[0], acc[1]), make_float2(v.x, v.y));
+        const float2 b = fadd2(make_float2(acc[2], acc[3]), make_float2(v.z, v.w));
+        acc[0] = a.x; acc[1] = a.y; acc[2] = b.x; acc[3] = b.y;
+    } else {
+        acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
+    }
+}
+
+template <bool PK, int C>
+__device__ __forceinline__ float2 div_pair(float2 a) {
+    if constexpr (PK) return div_fast2<C>(a);
+    else return make_float2(div_fast<C>(a.x), div_fast<C>(a.y));
 }
 
 constexpr int kTX = 128, kTY = 16, kNS = 16, kRA = 8;
@@ -80,6 +158,7 @@ __global__ void __launch_bounds__(LpShape<R>::THREADS, 1)
     using S = LpShape<R>;
     constexpr int C = 6 * R;
     constexpr int QN = 2 * R + 1;
+    constexpr bool PK = R >= 3;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char *ring = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
@@ -158,38 +237,27 @@ __global__ void __launch_bounds__(LpShape<R>::THREADS, 1)
                     rn = __ldg(reinterpret_cast<const uint2 *>(rhs + (long long)(z + 1) * g.sz + rowoff));
                 const int sc = (qb + step + R) & (kNS - 1);
                 const unsigned char *cb = ring + sc * S::SLOT_BYTES + own;
-                float w[12];  // cells x-4 .. x+7
+                // cells x-4 .. x+7 of row y as six 2-cell words; x- and y-neighbours
+                // are added straight from the 16-bit values (mixed-precision adds)
+                uint32_t wd[6];
                 {
-                    const float4 a = to4<E>(*reinterpret_cast<const uint2 *>(cb - 8));
-                    const float4 c = to4<E>(*reinterpret_cast<const uint2 *>(cb));
-                    const float4 b = to4<E>(*reinterpret_cast<const uint2 *>(cb + 8));
-                    w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w;
-                    w[4] = c.x; w[5] = c.y; w[6] = c.z; w[7] = c.w;
-                    w[8] = b.x; w[9] = b.y; w[10] = b.z; w[11] = b.w;
+                    const uint2 a = *reinterpret_cast<const uint2 *>(cb - 8);
+                    const uint2 c = *reinterpret_cast<const uint2 *>(cb);
+                    const uint2 b = *reinterpret_cast<const uint2 *>(cb + 8);
+                    wd[0] = a.x; wd[1] = a.y; wd[2] = c.x; wd[3] = c.y; wd[4] = b.x; wd[5] = b.y;
                 }
                 float acc[4];
-                // axis i (first term starts the sum)
-#pragma unroll
-                for (int e = 0; e < 4; ++e) acc[e] = w[4 + e - R];
-#pragma unroll
-                for (int o = -R + 1; o <= R; ++o) {
-                    if (!o) continue;
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) acc[e] += w[4 + e + o];
-                }
+                // axis i; the first term starts the sum (x + -0 = x exactly)
+                xsum<E, R>(wd, acc);
                 // axis j
 #pragma unroll
                 for (int o = -R; o <= R; ++o) {
                     if (!o) continue;
-                    const float4 v = to4<E>(*reinterpret_cast<const uint2 *>(cb + o * ROW));
-                    acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
+                    add_row<E>(*reinterpret_cast<const uint2 *>(cb + o * ROW), acc);
                 }
                 // axis k, planes z-R .. z-1
 #pragma unroll
-                for (int o = -R; o <= -1; ++o) {
-                    const float4 v = qz[(ph + R + o + QN) % QN];
-                    acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
-                }
+                for (int o = -R; o <= -1; ++o) add_q<PK>(qz[(ph + R + o + QN) % QN], acc);
                 release(sc);
                 {
                     const int pn = step + 2 * R;
@@ -201,18 +269,21 @@ __global__ void __launch_bounds__(LpShape<R>::THREADS, 1)
                     if (pn >= np - R) release(s);
                 }
 #pragma unroll
-                for (int o = 1; o <= R; ++o) {
-                    const float4 v = qz[(ph + R + o) % QN];
-                    acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
-                }
+                for (int o = 1; o <= R; ++o) add_q<PK>(qz[(ph + R + o) % QN], acc);
                 if (live) {
-                    const float4 r4 = to4<E>(rc);
-                    const float rv[4] = {r4.x, r4.y, r4.z, r4.w};
                     float out[4];
+                    const bool fast = div_fast_ok<C>(acc[0]) && div_fast_ok<C>(acc[1]) &&
+                                      div_fast_ok<C>(acc[2]) && div_fast_ok<C>(acc[3]);
+                    if (fast) {
+                        const float2 d0 = div_pair<PK, C>(make_float2(acc[0], acc[1]));
+                        const float2 d1 = div_pair<PK, C>(make_float2(acc[2], acc[3]));
+                        out[0] = d0.x; out[1] = d0.y; out[2] = d1.x; out[3] = d1.y;
+                    } else {
 #pragma unroll
-                    for (int e = 0; e < 4; ++e)
-                        out[e] = (div_fast_ok<C>(acc[e]) ? div_fast<C>(acc[e])
-                                                          : div_slow_from_first<C>(acc[e])) + rv[e];
+                        for (int e = 0; e < 4; ++e)
+                            out[e] = div_fast_ok<C>(acc[e]) ? div_fast<C>(acc[e]) : div_slow_from_first<C>(acc[e]);
+                    }
+                    add_row<E>(rc, out);  // + rhs
                     E *dst = eo + (long long)z * g.sz + rowoff;
                     if (xin) {
                         uint2 o2;
