@@ -244,3 +244,25 @@ def test_persistent_stream_matches_oracle(cuda, case, mode):
     got, u1, u2, res = gpu_run(u, radius, iters, mode, "coop", second, temporal=1)
     assert (res.data_ptr() == u1.data_ptr()) == (iters % 2 == 0)
     assert bits_equal(got, oracle_run(u, radius, iters, mode, second))
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("variant", ["auto", "base"])
+def test_grid_beyond_2_31_cells(cuda, variant):
+    """1296^3 = 2.18e9 cells (8.7 GB per buffer): 2 sweeps, then planes near
+    the middle and the far end (offsets beyond 2^31 cells) against the oracle
+    run on the 5-plane slab that determines them."""
+    import torch
+    from thesis_gb300 import stencil as S
+    n, R, iters = 1296, 1, 2
+    u = S.init_uniform((n, n, n), 77)
+    a, b = u.clone(), u.clone()
+    res = S.sweep(a, b, R, iters, O.JACOBI, variant)
+    torch.cuda.synchronize()
+    for z in (n // 2, n - 3):
+        slab = u[z - 2:z + 3].cpu().numpy()
+        want = oracle_run(slab, R, iters, O.JACOBI, threads=os.cpu_count() or 8)
+        got = res[z].cpu().numpy()
+        assert bits_equal(got, want[2]), z
+    del a, b, u, res
+    torch.cuda.empty_cache()
