@@ -44,6 +44,13 @@ UNET_API int unet_conv3x3_fwd(const unet_act *x, const void *w, const float *b,
  * y[p] = act(b + sum_tap w[tap] x[p + dilation * (ky-1, kx-1)]). */
 UNET_API int unet_conv3x3_fwd_dil(const unet_act *x, const void *w, const float *b,
                                   const unet_act *y, int relu, int dilation, stencil_stream_t stream);
+/* The same convolution on a chosen engine: 1 = tcgen05 (5th-generation tensor
+ * cores, FP32 accumulator in tensor memory), 2 = warp-level mma.sync, 0 = the
+ * library's default.  Both engines take the same views and weights and agree
+ * up to the FP32 summation order before the BF16 rounding. */
+UNET_API int unet_conv3x3_fwd_engine(const unet_act *x, const void *w, const float *b,
+                                     const unet_act *y, int relu, int dilation, int engine,
+                                     stencil_stream_t stream);
 /* wt[ci][ky][kx][co] = w[co][2-ky][2-kx][ci]: the weights of the data-gradient
  * convolution, so that dx = unet_conv3x3_fwd(dy, wt, NULL, dx, 0). */
 UNET_API int unet_flip_weights(const void *w, void *wt, int cout, int cin,

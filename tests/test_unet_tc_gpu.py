@@ -1,0 +1,50 @@
+"""The tcgen05 convolution engine (5th-generation tensor cores, accumulator
+in tensor memory) against the warp-level mma.sync engine and a torch float64
+reference, on the same BF16 inputs."""
+import ctypes
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [  # n, cin, cout, h, w, dilation
+    (1, 32, 32, 10, 9, 1), (2, 32, 64, 16, 24, 1), (2, 64, 128, 16, 16, 2), (1, 384, 128, 8, 16, 1),
+    (2, 256, 256, 16, 12, 4), (3, 96, 32, 12, 20, 1), (1, 32, 64, 1, 200, 1)]
+
+
+def run_engines(n, cin, cout, h, w, dil, relu, engines=(1, 2)):
+    import torch
+    from thesis_gb300 import unet as U
+    L = U._L()
+    g = torch.Generator().manual_seed(cin * 7 + cout + dil)
+    x = torch.randn(n, h, w, cin, generator=g).to(torch.bfloat16)
+    wt = (torch.randn(cout, 9, cin, generator=g) * 0.1).to(torch.bfloat16)
+    b = torch.randn(cout, generator=g).float()
+    xd, wd, bd = x.cuda(), wt.cuda(), b.cuda()
+    outs = {}
+    for engine in engines:
+        y = torch.full((n, h, w, cout), float("nan"), dtype=torch.bfloat16, device="cuda")
+        U._chk(L.unet_conv3x3_fwd_engine(ctypes.byref(U.view(xd)), U._p(wd), U._p(bd),
+                                         ctypes.byref(U.view(y)), relu, dil, engine, None),
+               "engine %d" % engine)
+        torch.cuda.synchronize()
+        outs[engine] = y.cpu().double()
+    X = x.double().permute(0, 3, 1, 2)
+    W = wt.double().reshape(cout, 3, 3, cin).permute(0, 3, 1, 2)
+    ref = torch.nn.functional.conv2d(X, W, b.double(), padding=dil, dilation=dil).permute(0, 2, 3, 1)
+    if relu:
+        ref = torch.relu(ref)
+    return outs, ref
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
+@pytest.mark.parametrize("relu", [0, 1])
+def test_tcgen05_conv_matches_mma_and_float64(cuda, shape, relu):
+    import torch
+    outs, ref = run_engines(*shape, relu)
+    scale = ref.abs().max().item()
+    for engine in (1, 2):
+        assert torch.isfinite(outs[engine]).all(), engine
+        assert (outs[engine] - ref).abs().max().item() / scale < 1e-2, engine
+    # the engines differ only by the FP32 summation order before the BF16 rounding
+    assert (outs[1] - outs[2]).abs().max().item() / scale < 1e-2

@@ -168,6 +168,218 @@ __global__ void __launch_bounds__(128)
 }
 
 // ---------------------------------------------------------------------------
+// 3x3 convolution, forward / data gradient, on the 5th-generation tensor
+// cores: tcgen05.mma (kind::f16, BF16 operands, FP32 accumulator in tensor
+// memory), issued by one thread, completion tracked by tcgen05.commit on an
+// mbarrier per shared-memory stage.
+//   D[128 pixels x BN channels] (TMEM, BN columns) += A[128 x 16] B[BN x 16]^T
+// per instruction; K runs over (tap, 32-channel chunk), two instructions per
+// chunk.  A (the shifted input pixels, zero outside the image) and B (the
+// weights of one tap and chunk) are staged by cp.async into a ring of
+// TC_STAGES buffers in the canonical K-major layout without swizzle: 8-row x
+// 16-byte core matrices, 128 bytes apart along K (leading byte offset) and
+// 512 bytes apart along M/N (stride byte offset).  The epilogue reads the
+// accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = pixels),
+// adds the bias, applies ReLU and stores BF16.  Every mbarrier wait is
+// bounded; a CTA that gives up waits (bounded) for its issued MMAs and frees
+// its TMEM.
+// ---------------------------------------------------------------------------
+// shared-memory stages: more for wide tiles, fewer (more resident CTAs) for narrow ones
+template <int BN>
+__host__ __device__ constexpr int tc_stages() { return BN >= 128 ? 6 : (BN >= 64 ? 4 : 3); }
+constexpr int TC_A_BYTES = BM * BK * 2;  // 8 KiB per stage
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+    // start address, leading byte offset 128 (K), stride byte offset 512
+    // (M/N), descriptor version 1, no swizzle
+    return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) |
+           ((uint64_t)(512 >> 4) << 32) | (1ull << 46);
+}
+
+template <int BN>
+__device__ __forceinline__ constexpr uint32_t umma_idesc() {
+    // D FP32, A and B BF16, both K-major, N = BN, M = 128
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+template <int BN>
+__global__ void __launch_bounds__(160)
+    k_conv3x3_tc(Act x, const bf16 *__restrict__ w, const float *__restrict__ bias, Act y, int relu,
+                 int dil) {
+    // warps 0-3: cp.async producers, then the epilogue (TMEM lanes 32w..32w+31);
+    // warp 4: one thread issues the MMAs
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    constexpr int B_BYTES = BN * BK * 2;
+    constexpr int TC_STAGES = tc_stages<BN>();
+    constexpr int LAG = TC_STAGES - 2;  // chunks in flight per producer before it signals
+    unsigned char *base = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(tc_smem) + 1023) & ~static_cast<uintptr_t>(1023));
+    unsigned char *As = base;
+    unsigned char *Bs = base + TC_STAGES * TC_A_BYTES;
+    uint64_t *full = reinterpret_cast<uint64_t *>(Bs + TC_STAGES * B_BYTES);
+    uint64_t *done = full + TC_STAGES;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(done + TC_STAGES);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long long P = (long long)x.n * x.h * x.w;
+    const long long m0 = (long long)blockIdx.x * BM;
+    const int n0 = blockIdx.y * BN;
+    const int cin = x.c, cout = y.c;
+    const int nc = cin / BK, KB = 9 * nc;
+
+    if (tid == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            mbar_init(&full[s], 128);
+            mbar_init(&done[s], 1);
+        }
+        fence_mbar_init();
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"(BN) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    bool ok = true;
+
+    if (warp < 4) {
+        // ---------------- producers ----------------
+        int a_n[4], a_y[4], a_x[4];
+        bool a_ok[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int row = (tid + 128 * i) >> 2;
+            const long long p = m0 + row;
+            a_ok[i] = p < P;
+            const long long pp = a_ok[i] ? p : 0;
+            a_x[i] = (int)(pp % x.w);
+            a_y[i] = (int)((pp / x.w) % x.h);
+            a_n[i] = (int)(pp / ((long long)x.w * x.h));
+        }
+        int signalled = 0;  // chunks whose copies this thread has reported complete
+        for (int k = 0; k < KB; ++k) {
+            const int st = k % TC_STAGES;
+            // the MMAs of chunk k - TC_STAGES read this stage last
+            if (k >= TC_STAGES && !mbar_wait_bounded(&done[st], ((k - TC_STAGES) / TC_STAGES) & 1)) {
+                ok = false;
+                break;
+            }
+            const int tap = k / nc, c0 = (k % nc) * BK;
+            const int dy = (tap / 3 - 1) * dil, dx = (tap % 3 - 1) * dil;
+            unsigned char *a = As + st * TC_A_BYTES;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int idx = tid + 128 * i, row = idx >> 2, part = idx & 3;
+                const int yy = a_y[i] + dy, xx = a_x[i] + dx;
+                const bool v = a_ok[i] && yy >= 0 && yy < x.h && xx >= 0 && xx < x.w;
+                const bf16 *src = x.p + (((long long)a_n[i] * x.h + (v ? yy : 0)) * x.w + (v ? xx : 0)) * x.cs +
+                                  x.co + c0 + part * 8;
+                cp_async16(a + (row >> 3) * 512 + part * 128 + (row & 7) * 16, src, v);
+            }
+            unsigned char *b = Bs + st * B_BYTES;
+#pragma unroll
+            for (int i = 0; i < (BN * 4) / 128; ++i) {
+                const int idx = tid + 128 * i, row = idx >> 2, part = idx & 3;
+                const int co = n0 + row;
+                const bool v = co < cout;
+                const bf16 *src = w + ((long long)(v ? co : 0) * 9 + tap) * cin + c0 + part * 8;
+                cp_async16(b + (row >> 3) * 512 + part * 128 + (row & 7) * 16, src, v);
+            }
+            cp_async_commit();
+            if (k >= LAG) {
+                // chunk k - LAG has landed: make it visible to the async proxy, report it
+                asm volatile("cp.async.wait_group %0;" ::"n"(LAG) : "memory");
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive(&full[(k - LAG) % TC_STAGES]);
+                signalled = k - LAG + 1;
+            }
+        }
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (ok)
+            for (int k = signalled; k < KB; ++k) mbar_arrive(&full[k % TC_STAGES]);
+    } else if (lane == 0) {
+        // ---------------- MMA issuer ----------------
+        constexpr uint32_t IDESC = umma_idesc<BN>();
+        int issued = 0;
+        for (int k = 0; k < KB; ++k) {
+            const int st = k % TC_STAGES;
+            if (!mbar_wait_bounded(&full[st], (k / TC_STAGES) & 1)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t a = smem_u32(As + st * TC_A_BYTES), b = smem_u32(Bs + st * B_BYTES);
+#pragma unroll
+            for (int j = 0; j < BK / 16; ++j) {
+                const uint64_t ad = umma_desc(a + j * 256), bd = umma_desc(b + j * 256);
+                const uint32_t acc = (k > 0 || j > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(&done[st]))
+                         : "memory");
+            issued = k + 1;
+        }
+        // every issued MMA has completed once the last commit has arrived
+        if (issued > 0 &&
+            !mbar_wait_bounded(&done[(issued - 1) % TC_STAGES], ((issued - 1) / TC_STAGES) & 1))
+            ok = false;
+        if (issued < KB) ok = false;
+    }
+    tc_fence_before();
+    ok = __syncthreads_and(ok);
+    tc_fence_after();
+    if (ok && warp < 4) {
+        const long long p = m0 + warp * 32 + lane;
+#pragma unroll
+        for (int c = 0; c < BN; c += 8) {
+            uint32_t r[8];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                  "=r"(r[7])
+                : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            const int co = n0 + c;
+            if (p < P && co < cout) {
+                float v[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    v[e] = __uint_as_float(r[e]) + (bias ? bias[co + e] : 0.f);
+                    if (relu) v[e] = fmaxf(v[e], 0.f);
+                }
+                uint4 q;
+                __nv_bfloat162 h0 = __floats2bfloat162_rn(v[0], v[1]), h1 = __floats2bfloat162_rn(v[2], v[3]);
+                __nv_bfloat162 h2 = __floats2bfloat162_rn(v[4], v[5]), h3 = __floats2bfloat162_rn(v[6], v[7]);
+                q.x = *reinterpret_cast<uint32_t *>(&h0);
+                q.y = *reinterpret_cast<uint32_t *>(&h1);
+                q.z = *reinterpret_cast<uint32_t *>(&h2);
+                q.w = *reinterpret_cast<uint32_t *>(&h3);
+                *reinterpret_cast<uint4 *>(y.p + p * y.cs + y.co + co) = q;
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+    }
+}
+
+template <int BN>
+constexpr int tc_smem_bytes() {
+    return tc_stages<BN>() * (TC_A_BYTES + BN * BK * 2) + 2 * tc_stages<BN>() * 8 + 16 + 1024;
+}
+
+// ---------------------------------------------------------------------------
 // Weight gradient: dW[co][tap][ci] += sum_p dy[p][co] x[p + tap][ci].
 // Block: 128 threads = 2 x 2 warps, tile 64 (co) x 64 (ci), K = pixels in
 // chunks of 32 from this block's pixel range; grid.z = tap.
@@ -616,17 +828,45 @@ using namespace st;
     do { int rc_ = check_act(v, #v); if (rc_) return rc_; } while (0)
 #define STREAM(s) reinterpret_cast<cudaStream_t>(s)
 
-extern "C" int unet_conv3x3_fwd_dil(const unet_act *x, const void *w, const float *b,
-                                    const unet_act *y, int relu, int dilation, stencil_stream_t s) {
+template <int BN>
+int launch_conv_tc(const Act &xa, const bf16 *wb, const float *b, const Act &ya, int relu, int dil,
+                   long long P, cudaStream_t s) {
+    static bool attr[64] = {false};
+    const int dev = current_device();
+    if (dev >= 0 && dev < 64 && !attr[dev]) {
+        ST_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     tc_smem_bytes<BN>()));
+        attr[dev] = true;
+    }
+    dim3 grid((unsigned)((P + BM - 1) / BM), ya.c / BN);
+    k_conv3x3_tc<BN><<<grid, 160, tc_smem_bytes<BN>(), s>>>(xa, wb, b, ya, relu, dil);
+    return cuda_fail(cudaGetLastError(), "conv3x3 (tcgen05) launch");
+}
+
+extern "C" int unet_conv3x3_fwd_engine(const unet_act *x, const void *w, const float *b,
+                                       const unet_act *y, int relu, int dilation, int engine,
+                                       stencil_stream_t s) {
     CHECK_VIEW(x);
     CHECK_VIEW(y);
     if (!w) return fail(STENCIL_EINVAL, "null weights");
     if (dilation < 1) return fail(STENCIL_EINVAL, "dilation must be >= 1");
+    if (engine < 0 || engine > 2) return fail(STENCIL_EINVAL, "engine must be 0, 1 or 2");
     if (x->c % 32 || y->c % 32) return fail(STENCIL_EINVAL, "channels must be multiples of 32");
     if (x->n != y->n || x->h != y->h || x->w != y->w) return fail(STENCIL_EINVAL, "shape mismatch");
     const long long P = (long long)x->n * x->h * x->w;
     const Act xa = to_act(*x), ya = to_act(*y);
     const bf16 *wb = static_cast<const bf16 *>(w);
+    // default: tcgen05 where it measured at least as fast as mma.sync on
+    // GB300 -- wide tiles with long K (128 output channels x 384 inputs: 225
+    // vs 220 TFLOP/s; 256 x 256: 207 vs 191); shorter or narrower layers are
+    // bound by the cp.async operand staging both engines share, where the
+    // mma.sync kernel keeps more CTAs resident (32 x 32: 129 vs 75)
+    if (engine == 0) engine = (y->c % 128 == 0 && x->c >= 256) ? 1 : 2;
+    if (engine == 1) {
+        if (y->c % 128 == 0) return launch_conv_tc<128>(xa, wb, b, ya, relu, dilation, P, STREAM(s));
+        if (y->c % 64 == 0) return launch_conv_tc<64>(xa, wb, b, ya, relu, dilation, P, STREAM(s));
+        return launch_conv_tc<32>(xa, wb, b, ya, relu, dilation, P, STREAM(s));
+    }
     if (y->c % 64 == 0) {
         dim3 grid((unsigned)((P + BM - 1) / BM), y->c / 64);
         k_conv3x3<64><<<grid, 128, 0, STREAM(s)>>>(xa, wb, b, ya, relu, dilation);
@@ -635,6 +875,11 @@ extern "C" int unet_conv3x3_fwd_dil(const unet_act *x, const void *w, const floa
         k_conv3x3<32><<<grid, 128, 0, STREAM(s)>>>(xa, wb, b, ya, relu, dilation);
     }
     return cuda_fail(cudaGetLastError(), "conv3x3 launch");
+}
+
+extern "C" int unet_conv3x3_fwd_dil(const unet_act *x, const void *w, const float *b,
+                                    const unet_act *y, int relu, int dilation, stencil_stream_t s) {
+    return unet_conv3x3_fwd_engine(x, w, b, y, relu, dilation, 0, s);
 }
 
 extern "C" int unet_conv3x3_fwd(const unet_act *x, const void *w, const float *b, const unet_act *y,

@@ -49,6 +49,19 @@ def main(case):
         u = S.init_fourier((384, 384, 384), 1, 4)
         for _ in range(2):
             S.ir_solve(u, 4, 8, "bf16", inner_sweeps=8)
+    elif case in ("conv_tc", "conv_mma"):
+        # one U-Net layer shape (d2a: 32^2, 384 -> 128 channels, batch 64) on each engine
+        import ctypes
+        from . import unet as U
+        L = U._L()
+        x = torch.randn(64, 32, 32, 384, device="cuda").to(torch.bfloat16)
+        w = (torch.randn(128, 9, 384, device="cuda") * 0.05).to(torch.bfloat16)
+        b = torch.zeros(128, device="cuda")
+        y = torch.empty(64, 32, 32, 128, dtype=torch.bfloat16, device="cuda")
+        eng = 1 if case == "conv_tc" else 2
+        for _ in range(4):
+            U._chk(L.unet_conv3x3_fwd_engine(ctypes.byref(U.view(x)), U._p(w), U._p(b),
+                                             ctypes.byref(U.view(y)), 1, 1, eng, None), case)
     elif case == "unet_train":
         from .unet import UNet
         from . import warmstart as W

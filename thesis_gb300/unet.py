@@ -59,6 +59,7 @@ def _L():
         sig = {
             "unet_conv3x3_fwd": [A, vp, vp, A, i, vp],
             "unet_conv3x3_fwd_dil": [A, vp, vp, A, i, i, vp],
+            "unet_conv3x3_fwd_engine": [A, vp, vp, A, i, i, i, vp],
             "unet_conv3x3_wgrad_dil": [A, A, vp, vp, i, vp],
             "unet_flip_weights": [vp, vp, i, i, vp],
             "unet_conv3x3_wgrad": [A, A, vp, vp, vp],
