@@ -441,9 +441,12 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     // re-reads hit L2.  The chunk count is chosen so the items fill whole
     // waves of resident CTAs (a partly filled last wave idles SMs) while
     // chunks stay long (each re-reads 2R halo planes and re-primes the queue).
+    // Chunks may be as short as 2 planes: on small grids a long chunk is a
+    // long chain of dependent plane steps on few CTAs (96^3 R=2: 11 us per
+    // sweep with 9-plane chunks on 33 CTAs).
     int nchunks = 1;
     double best = 1e30;
-    for (int n = 1; n <= std::max(1, zin / 8); ++n) {
+    for (int n = 1; n <= std::max(1, zin / 2); ++n) {
         const int zc = (zin + n - 1) / n;
         const long long it = (long long)tiles * ((zin + zc - 1) / zc);
         const double waves = std::ceil((double)it / resident);
