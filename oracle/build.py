@@ -81,8 +81,13 @@ def build_ref(configs, jobs: int = 8) -> list[str]:
 # comparison.
 REF_GPU_SHAPES_512 = [(32, 4, 4, 1), (32, 8, 4, 1), (64, 4, 4, 1), (32, 8, 2, 1), (32, 4, 4, 2),
                       (32, 8, 2, 4)]
+# 2-D 256^2 R=1 (the 1000-sweep configuration), and a 64^2 parity case
+REF_GPU_SHAPES_256 = [(32, 8, 1, 1), (32, 4, 1, 1), (64, 4, 1, 1), (32, 16, 1, 1), (32, 8, 1, 2),
+                      (64, 8, 1, 1), (128, 2, 1, 1)]
 REF_GPU_CONFIGS = ([(3, 64, r, 32, 4, 4, 1) for r in (1, 2)] + [(3, 64, 2, 32, 4, 4, 2)] +
-                   [(3, 512, r, bx, by, bz, cf) for r in (1, 4) for (bx, by, bz, cf) in REF_GPU_SHAPES_512])
+                   [(3, 512, r, bx, by, bz, cf) for r in (1, 4) for (bx, by, bz, cf) in REF_GPU_SHAPES_512] +
+                   [(2, 64, 1, 32, 8, 1, 1)] +
+                   [(2, 256, 1, bx, by, bz, cf) for (bx, by, bz, cf) in REF_GPU_SHAPES_256])
 
 
 def ref_cubin(cfg) -> str:

@@ -25,7 +25,8 @@ def bits_equal(a, b):
 
 GOLDEN_CFGS = [((3, 64, 1, 32, 4, 4, 1), "legacy_3d_64_r1_i8.npz"),
                ((3, 64, 2, 32, 4, 4, 1), "legacy_3d_64_r2_i8.npz"),
-               ((3, 64, 2, 32, 4, 4, 2), "legacy_3d_64_r2_i8.npz")]
+               ((3, 64, 2, 32, 4, 4, 2), "legacy_3d_64_r2_i8.npz"),
+               ((2, 64, 1, 32, 8, 1, 1), "legacy_2d_64_r1_i8.npz")]
 
 
 @pytest.mark.parametrize("cfg,golden", GOLDEN_CFGS, ids=lambda x: str(x))
@@ -101,3 +102,72 @@ def test_library_beats_reference_kernels_512(cuda, radius):
     for v, variant, shape in rows:
         print("  reference %-14s block %dx%dx%d cf %d: %.1f GCell/s" % ((variant,) + shape + (v,)))
     assert ours > rows[0][0]
+
+
+def test_library_beats_reference_kernels_2d_256(cuda):
+    """2-D 256^2 R=1, 1000 sweeps (the reference's 2-D configuration), LEGACY
+    from the reference's initial state: every reference kernel x block shape
+    built for it against the library's AUTO engine (one cluster launch),
+    bit for bit and in time."""
+    import torch
+    from thesis_gb300 import lib, stencil as S
+    cfgs = [c for c in OB.REF_GPU_CONFIGS if c[0] == 2 and c[1] == 256]
+    if not all(G.available(c) for c in cfgs):
+        pytest.skip("reference cubins not built")
+    n, radius, sweeps = 256, 1, 1000
+    u = torch.from_numpy(O.init_reference((n, n))).cuda()
+    a, b = u.clone(), torch.zeros_like(u)
+    def timed(run):
+        run()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            run()
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best
+
+    def ours():
+        a.copy_(u)
+        b.zero_()
+        return S.sweep(a, b, radius, sweeps, lib.MODE_LEGACY, "auto")
+
+    ms_ours = timed(ours)
+    want = ours().clone()
+    rows = []
+    for cfg in cfgs:
+        kern = G.RefKernels(cfg)
+        for variant in G.VARIANTS:
+            if not G.valid(variant, cfg[0], cfg[2], cfg[3], cfg[4], cfg[5]):
+                continue
+
+            # the 1000 launches replayed from a CUDA graph: the reference
+            # kernels without any host launch overhead
+            graph, gs = torch.cuda.CUDAGraph(), torch.cuda.Stream()
+            a.copy_(u)
+            b.zero_()
+            torch.cuda.synchronize()
+            with torch.cuda.stream(gs):
+                with torch.cuda.graph(graph, stream=gs):
+                    res = kern.sweeps(variant, a.data_ptr(), b.data_ptr(), sweeps, gs.cuda_stream)
+
+            def ref():
+                a.copy_(u)
+                b.zero_()
+                graph.replay()
+
+            ref()
+            torch.cuda.synchronize()
+            got = a if res == a.data_ptr() else b
+            assert torch.equal(got.view(torch.int32), want.view(torch.int32)), (variant, cfg)
+            rows.append((timed(ref), variant, tuple(cfg[3:])))
+            del graph
+        kern.close()
+    rows.sort()
+    print("\n256^2 R=1 LEGACY, 1000 sweeps: library %.3f ms (reference kernels replayed from CUDA graphs)" % ms_ours)
+    for ms, variant, shape in rows:
+        print("  reference %-14s block %dx%dx%d cf %d: %.3f ms" % ((variant,) + shape + (ms,)))
+    assert ms_ours < rows[0][0]
