@@ -1,6 +1,7 @@
 """The tcgen05 convolution engine (5th-generation tensor cores, accumulator
-in tensor memory) against the warp-level mma.sync engine and a torch float64
-reference, on the same BF16 inputs."""
+in tensor memory; TMA-fed operands where the 128-pixel tiles are whole image
+rows or row runs, cp.async-fed otherwise) against the warp-level mma.sync
+engine and a torch float64 reference, on the same BF16 inputs."""
 import ctypes
 
 import pytest
@@ -9,7 +10,10 @@ pytestmark = pytest.mark.gpu
 
 SHAPES = [  # n, cin, cout, h, w, dilation
     (1, 32, 32, 10, 9, 1), (2, 32, 64, 16, 24, 1), (2, 64, 128, 16, 16, 2), (1, 384, 128, 8, 16, 1),
-    (2, 256, 256, 16, 12, 4), (3, 96, 32, 12, 20, 1), (1, 32, 64, 1, 200, 1)]
+    (2, 256, 256, 16, 12, 4), (3, 96, 32, 12, 20, 1), (1, 32, 64, 1, 200, 1),
+    # shapes whose 128-pixel tiles are whole rows or row runs: TMA-fed operands
+    (2, 32, 32, 128, 128, 1), (1, 96, 32, 64, 64, 1), (2, 128, 128, 32, 32, 1), (1, 32, 64, 4, 256, 1),
+    (1, 256, 256, 16, 16, 4), (3, 192, 64, 8, 64, 1)]
 
 
 def run_engines(n, cin, cout, h, w, dil, relu, engines=(1, 2)):

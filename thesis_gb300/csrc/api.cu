@@ -119,6 +119,26 @@ int make_tensor_map_typed(CUtensorMap *map, const void *base, int rank, const lo
     return STENCIL_OK;
 }
 
+int make_tensor_map_general(CUtensorMap *map, CUtensorMapDataType dtype, int rank, const void *base,
+                            const unsigned long long *dims, const unsigned long long *strides,
+                            const unsigned *box, CUtensorMapSwizzle swizzle) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return fail(STENCIL_ECUDA, "cuTensorMapEncodeTiled is unavailable");
+    if (rank < 1 || rank > 5) return fail(STENCIL_EINVAL, "tensor map rank %d", rank);
+    cuuint64_t gdim[5], gstride[4];
+    cuuint32_t bdim[5], estride[5] = {1, 1, 1, 1, 1};
+    for (int i = 0; i < rank; ++i) {
+        gdim[i] = (cuuint64_t)dims[i];
+        bdim[i] = (cuuint32_t)box[i];
+        if (i + 1 < rank) gstride[i] = (cuuint64_t)strides[i];
+    }
+    CUresult r = fn(map, dtype, (cuuint32_t)rank, const_cast<void *>(base), gdim, gstride, bdim, estride,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(STENCIL_EINVAL, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return STENCIL_OK;
+}
+
 int make_tensor_map(CUtensorMap *map, const float *base, int rank, const long long *dims,
                     const int *box) {
     return make_tensor_map_typed(map, base, rank, dims, box, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4);

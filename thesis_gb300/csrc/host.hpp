@@ -30,6 +30,10 @@ int current_device();
 // Builds a tiled TMA descriptor for an FP32 grid (rank 2 or 3).
 int make_tensor_map(CUtensorMap *map, const float *base, int rank, const long long *dims,
                     const int *box);
+// Any rank (1..5), element type, byte strides of dims 1.. and swizzle.
+int make_tensor_map_general(CUtensorMap *map, CUtensorMapDataType dtype, int rank, const void *base,
+                            const unsigned long long *dims, const unsigned long long *strides,
+                            const unsigned *box, CUtensorMapSwizzle swizzle);
 // The same for another element type (e.g. BF16/FP16 grids, 2 bytes).
 int make_tensor_map_typed(CUtensorMap *map, const void *base, int rank, const long long *dims,
                           const int *box, CUtensorMapDataType dtype, int elem_bytes);
