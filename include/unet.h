@@ -64,6 +64,17 @@ UNET_API int unet_conv3x3_wgrad(const unet_act *x, const unet_act *dy, float *dw
  * same dilation. */
 UNET_API int unet_conv3x3_wgrad_dil(const unet_act *x, const unet_act *dy, float *dw, float *db,
                                     int dilation, stencil_stream_t stream);
+/* Bytes of device workspace the tcgen05 weight gradient needs for these
+ * views: channel-major copies of x (three, shifted by -dilation, 0 and
+ * +dilation columns) and of dy: (3 x->c + dy->c) * n * h * w * 2. */
+UNET_API int unet_wgrad_workspace_bytes(const unet_act *x, const unet_act *dy, size_t *bytes);
+/* The weight gradient on a chosen engine: 1 = tcgen05 (TMEM accumulator,
+ * TMA-fed operands; needs w % 32 == 0 and a 256-byte aligned workspace of
+ * unet_wgrad_workspace_bytes), 2 = mma.sync, 0 = tcgen05 where it applies.
+ * Same accumulation contract as unet_conv3x3_wgrad_dil (FP32 atomics). */
+UNET_API int unet_conv3x3_wgrad_engine(const unet_act *x, const unet_act *dy, float *dw, float *db,
+                                       int dilation, int engine, void *workspace,
+                                       size_t workspace_bytes, stencil_stream_t stream);
 /* g *= (y > 0), element-wise over the view. */
 UNET_API int unet_relu_bwd(const unet_act *g, const unet_act *y, stencil_stream_t stream);
 /* 2x2 max pooling (h, w even) and its gradient (to the first maximal input). */

@@ -52,3 +52,44 @@ def test_tcgen05_conv_matches_mma_and_float64(cuda, shape, relu):
         assert (outs[engine] - ref).abs().max().item() / scale < 1e-2, engine
     # the engines differ only by the FP32 summation order before the BF16 rounding
     assert (outs[1] - outs[2]).abs().max().item() / scale < 1e-2
+
+
+WG_SHAPES = [  # n, cin, cout, h, w, dilation
+    (2, 32, 32, 16, 32, 1), (1, 96, 32, 8, 64, 1), (2, 64, 128, 8, 32, 1), (1, 384, 128, 4, 32, 1),
+    (2, 256, 256, 8, 32, 4), (1, 128, 256, 16, 32, 2), (3, 32, 64, 5, 96, 1)]
+
+
+@pytest.mark.parametrize("shape", WG_SHAPES, ids=lambda s: "x".join(map(str, s)))
+def test_tcgen05_weight_gradient_matches_mma_and_float64(cuda, shape):
+    import torch
+    from thesis_gb300 import unet as U
+    n, cin, cout, h, w, dil = shape
+    L = U._L()
+    g = torch.Generator().manual_seed(cin + 3 * cout + dil)
+    x = torch.randn(n, h, w, cin, generator=g).to(torch.bfloat16)
+    dy = torch.randn(n, h, w, cout, generator=g).to(torch.bfloat16)
+    xd, dyd = x.cuda(), dy.cuda()
+    need = ctypes.c_size_t()
+    U._chk(L.unet_wgrad_workspace_bytes(ctypes.byref(U.view(xd)), ctypes.byref(U.view(dyd)),
+                                        ctypes.byref(need)), "ws")
+    ws = torch.empty(need.value, dtype=torch.uint8, device="cuda")
+    outs = {}
+    for engine in (1, 2):
+        dw = torch.zeros(cout, 9, cin, device="cuda")
+        db = torch.zeros(cout, device="cuda")
+        for _ in range(2):  # accumulates: two calls give twice the gradient
+            U._chk(L.unet_conv3x3_wgrad_engine(ctypes.byref(U.view(xd)), ctypes.byref(U.view(dyd)),
+                                               U._p(dw), U._p(db), dil, engine, U._p(ws), need.value,
+                                               None), "wgrad %d" % engine)
+        torch.cuda.synchronize()
+        outs[engine] = (dw.cpu().double() / 2, db.cpu().double() / 2)
+    X = x.double().permute(0, 3, 1, 2).requires_grad_(True)
+    W = torch.zeros(cout, cin, 3, 3, dtype=torch.float64, requires_grad=True)
+    out = torch.nn.functional.conv2d(X, W, None, padding=dil, dilation=dil)
+    out.backward(dy.double().permute(0, 3, 1, 2))
+    ref = W.grad.permute(0, 2, 3, 1).reshape(cout, 9, cin)
+    refb = dy.double().sum((0, 1, 2))
+    for engine in (1, 2):
+        gw, gb = outs[engine]
+        assert (gw - ref).abs().max().item() / ref.abs().max().item() < 1e-4, engine
+        assert (gb - refb).abs().max().item() / refb.abs().max().item() < 1e-4, engine

@@ -537,6 +537,190 @@ constexpr int tma_smem_bytes() {
     return TMA_STAGES * (TC_A_BYTES + BN * BK * 2) + (2 * TMA_STAGES + 1) * 8 + 16 + 1024;
 }
 
+// ---------------------------------------------------------------------------
+// Weight gradient on tcgen05:
+//   dW[co][tap][ci] += sum_p dy[p][co] x[p + tap][ci]
+// as per-tap GEMMs D[co][ci] (M = 128 output channels, N = BN input
+// channels) with K = pixels in 32-pixel chunks (a run of one image row),
+// accumulated in TMEM over the CTA's slice of the pixels and added to dW
+// with FP32 atomics.  Both operands must be K-major (pixels contiguous), so
+// dy and x are first transposed into channel-major copies (k_to_cmajor) in
+// the caller's workspace; a chunk is then one 4-D tensor-map box per operand
+// (the x box shifted by the tap, out-of-bounds zeros = the padding), 64-byte
+// swizzle, the same UMMA descriptors as the forward kernel.  Warps: 0-3
+// epilogue, 4 TMA producer, 5 MMA issuer.
+// ---------------------------------------------------------------------------
+// out[c][p] = view[p shifted by dx columns][c], zero where the shifted
+// column leaves the image (32 x 32 tiles through shared memory; W % 32 == 0,
+// so a 32-pixel tile lies in one image row).  The shift is applied here, not
+// by the tensor map, because a TMA box may only start at a 16-byte aligned
+// innermost coordinate and the pixels are the innermost dimension.
+__global__ void __launch_bounds__(256) k_to_cmajor(Act a, bf16 *__restrict__ out, long long P, int W, int dx) {
+    // tile: 64 pixels x 32 channels; 16-byte loads (8 channels of a pixel)
+    // and 16-byte stores (8 pixels of a channel)
+    __shared__ __align__(16) bf16 t[32][64 + 8];
+    const long long p0 = (long long)blockIdx.x * 64;
+    const int c0 = blockIdx.y * 32;
+    const int tid = threadIdx.x;
+    {
+        const int r = tid >> 2, q = tid & 3;
+        const long long p = p0 + r;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (p < P) {
+            const int ws = (int)(p % W) + dx;
+            if (ws >= 0 && ws < W)
+                v = *reinterpret_cast<const uint4 *>(a.p + (p + dx) * a.cs + a.co + c0 + 8 * q);
+        }
+        const bf16 *e = reinterpret_cast<const bf16 *>(&v);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) t[8 * q + k][r] = e[k];
+    }
+    __syncthreads();
+    {
+        const int c = tid >> 3, q = tid & 7;
+        const long long p = p0 + 8 * q;
+        if (p + 8 <= P) {
+            *reinterpret_cast<uint4 *>(out + (long long)(c0 + c) * P + p) =
+                *reinterpret_cast<const uint4 *>(&t[c][8 * q]);
+        } else {
+            for (int k = 0; k < 8 && p + k < P; ++k) out[(long long)(c0 + c) * P + p + k] = t[c][8 * q + k];
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0,
+                                            int c1, int c2, int c3, int c4) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%3, %4, %5, %6, %7}], [%2];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3),
+        "r"(c4)
+        : "memory");
+}
+
+template <int BN>
+__global__ void __launch_bounds__(192)
+    k_wgrad_tma(const __grid_constant__ CUtensorMap gmap, const __grid_constant__ CUtensorMap xmap,
+                float *__restrict__ dw, int cin, int cout, int H, int W, int dil, int chunks_per_cta,
+                long long nchunks) {
+    extern __shared__ __align__(1024) unsigned char wg_smem[];
+    constexpr int A_BYTES = BM * BK * 2;
+    constexpr int B_BYTES = BN * BK * 2;
+    constexpr int STAGE = A_BYTES + B_BYTES;
+    unsigned char *base = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(wg_smem) + 1023) & ~static_cast<uintptr_t>(1023));
+    uint64_t *full = reinterpret_cast<uint64_t *>(base + TMA_STAGES * STAGE);
+    uint64_t *empty = full + TMA_STAGES;
+    uint64_t *accd = empty + TMA_STAGES;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(accd + 1);
+    int *bad = reinterpret_cast<int *>(tslot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int co0 = blockIdx.x * BM, ci0 = blockIdx.y * BN;
+    const int tap = blockIdx.z % 9;
+    const long long k0 = (long long)(blockIdx.z / 9) * chunks_per_cta;
+    const int KB = (int)min((long long)chunks_per_cta, nchunks - k0);
+    const int dy = (tap / 3 - 1) * dil;
+    const int rowchunks = W / BK;  // 32-pixel chunks per image row
+
+    if (tid == 0) {
+        prefetch_tensormap(&gmap);
+        prefetch_tensormap(&xmap);
+        for (int s = 0; s < TMA_STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(accd, 1);
+        *bad = 0;
+        fence_mbar_init();
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"(BN) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    if (warp == 4) {
+        if (lane == 0) {
+            for (int k = 0; k < KB; ++k) {
+                const int st = k % TMA_STAGES;
+                if (k >= TMA_STAGES && !mbar_wait_bounded(&empty[st], ((k / TMA_STAGES) - 1) & 1)) {
+                    *bad = 1;
+                    break;
+                }
+                const long long ch = k0 + k;  // chunk = (n, h, 32-pixel run of the row)
+                const int wc = (int)(ch % rowchunks);
+                const long long r = ch / rowchunks;
+                const int h = (int)(r % H), n = (int)(r / H);
+                unsigned char *a = base + st * STAGE;
+                mbar_arrive_expect_tx(&full[st], STAGE);
+                tma_load_4d(a, &gmap, &full[st], wc * BK, h, n, co0);
+                // x copy shifted by this tap's column offset (index tap % 3), row shift by coordinate
+                tma_load_5d(a + A_BYTES, &xmap, &full[st], wc * BK, h + dy, n, ci0, tap % 3);
+            }
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {
+            constexpr uint32_t IDESC = umma_idesc<BN>();
+            for (int k = 0; k < KB; ++k) {
+                const int st = k % TMA_STAGES;
+                if (!mbar_wait_bounded(&full[st], (k / TMA_STAGES) & 1)) {
+                    *bad = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t a = smem_u32(base + st * STAGE), b = a + A_BYTES;
+#pragma unroll
+                for (int j = 0; j < BK / 16; ++j) {
+                    const uint64_t ad = umma_desc_sw64(a + j * 32), bd = umma_desc_sw64(b + j * 32);
+                    const uint32_t acc = (k > 0 || j > 0) ? 1u : 0u;
+                    asm volatile(
+                        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+                        "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
+                        : "memory");
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_u32(&empty[st]))
+                             : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(accd))
+                         : "memory");
+        }
+    } else {
+        const bool done = mbar_wait_bounded(accd, 0);
+        tc_fence_after();
+        if (done && KB > 0 && !*reinterpret_cast<volatile int *>(bad)) {
+            const int co = co0 + warp * 32 + lane;
+#pragma unroll
+            for (int c = 0; c < BN; c += 8) {
+                uint32_t r[8];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                      "=r"(r[7])
+                    : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (co < cout) {
+                    float *d = dw + ((long long)co * 9 + tap) * cin + ci0 + c;
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) atomicAdd(d + e, __uint_as_float(r[e]));
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+    }
+}
+
 template <int BN>
 constexpr int tc_smem_bytes() {
     return tc_stages<BN>() * (TC_A_BYTES + BN * BK * 2) + 2 * tc_stages<BN>() * 8 + 16 + 1024;
@@ -1104,6 +1288,90 @@ extern "C" int unet_flip_weights(const void *w, void *wt, int cout, int cin, ste
     k_flip<<<grid_for((long long)cout * 9 * cin), 256, 0, STREAM(s)>>>(
         static_cast<const bf16 *>(w), static_cast<bf16 *>(wt), cout, cin);
     return cuda_fail(cudaGetLastError(), "flip launch");
+}
+
+template <int BN>
+int launch_wgrad_tma(const unet_act *x, const unet_act *dy, float *dw, int dil, void *ws, cudaStream_t s) {
+    static bool attr[64] = {false};
+    constexpr int SMEM = TMA_STAGES * (BM * BK * 2 + BN * BK * 2) + (2 * TMA_STAGES + 1) * 8 + 16 + 1024;
+    const int dev = current_device();
+    if (dev >= 0 && dev < 64 && !attr[dev]) {
+        ST_CUDA(cudaFuncSetAttribute(k_wgrad_tma<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
+        attr[dev] = true;
+    }
+    const int cin = x->c, cout = dy->c, H = x->h, W = x->w, N = x->n;
+    const long long P = (long long)N * H * W;
+    // workspace: x as three channel-major copies shifted by -dil, 0, +dil
+    // columns, then dy channel-major
+    bf16 *xT = static_cast<bf16 *>(ws);
+    bf16 *gT = xT + 3LL * cin * P;
+    for (int k = 0; k < 3; ++k)
+        k_to_cmajor<<<dim3((unsigned)((P + 63) / 64), cin / 32), 256, 0, s>>>(
+            to_act(*x), xT + (long long)k * cin * P, P, W, (k - 1) * dil);
+    k_to_cmajor<<<dim3((unsigned)((P + 63) / 64), cout / 32), 256, 0, s>>>(to_act(*dy), gT, P, W, 0);
+    ST_CUDA(cudaGetLastError());
+    CUtensorMap gm, xm;
+    const unsigned long long p2 = (unsigned long long)P * 2;
+    const unsigned long long gd[4] = {(unsigned long long)W, (unsigned long long)H, (unsigned long long)N,
+                                      (unsigned long long)cout};
+    const unsigned long long st[4] = {(unsigned long long)W * 2, (unsigned long long)W * H * 2, p2,
+                                      p2 * (unsigned long long)cin};
+    const unsigned gb[4] = {(unsigned)BK, 1u, 1u, (unsigned)BM};
+    int rc = make_tensor_map_general(&gm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, gT, gd, st, gb,
+                                     CU_TENSOR_MAP_SWIZZLE_64B);
+    if (rc) return rc;
+    const unsigned long long xd[5] = {(unsigned long long)W, (unsigned long long)H, (unsigned long long)N,
+                                      (unsigned long long)cin, 3ull};
+    const unsigned xb[5] = {(unsigned)BK, 1u, 1u, (unsigned)BN, 1u};
+    rc = make_tensor_map_general(&xm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, xT, xd, st, xb,
+                                 CU_TENSOR_MAP_SWIZZLE_64B);
+    if (rc) return rc;
+    const long long nchunks = P / BK;
+    const int tiles = ((cout + BM - 1) / BM) * (cin / BN) * 9;
+    long long splits = (2LL * num_sms() + tiles - 1) / tiles;
+    long long per = (nchunks + splits - 1) / splits;
+    if (per < 16) per = 16;
+    splits = (nchunks + per - 1) / per;
+    dim3 grid((unsigned)((cout + BM - 1) / BM), (unsigned)(cin / BN), (unsigned)(9 * splits));
+    k_wgrad_tma<BN><<<grid, 192, SMEM, s>>>(gm, xm, dw, cin, cout, H, W, dil, (int)per, nchunks);
+    return cuda_fail(cudaGetLastError(), "wgrad (tcgen05) launch");
+}
+
+extern "C" int unet_wgrad_workspace_bytes(const unet_act *x, const unet_act *dy, size_t *bytes) {
+    CHECK_VIEW(x);
+    CHECK_VIEW(dy);
+    if (!bytes) return fail(STENCIL_EINVAL, "null bytes");
+    *bytes = (size_t)(3 * x->c + dy->c) * (size_t)x->n * x->h * x->w * 2;
+    return STENCIL_OK;
+}
+
+extern "C" int unet_conv3x3_wgrad_engine(const unet_act *x, const unet_act *dy, float *dw, float *db,
+                                         int dilation, int engine, void *workspace,
+                                         size_t workspace_bytes, stencil_stream_t s) {
+    CHECK_VIEW(x);
+    CHECK_VIEW(dy);
+    if (!dw) return fail(STENCIL_EINVAL, "null dw");
+    if (dilation < 1) return fail(STENCIL_EINVAL, "dilation must be >= 1");
+    if (engine < 0 || engine > 2) return fail(STENCIL_EINVAL, "engine must be 0, 1 or 2");
+    if (x->n != dy->n || x->h != dy->h || x->w != dy->w) return fail(STENCIL_EINVAL, "shape mismatch");
+    const size_t need = (size_t)(3 * x->c + dy->c) * (size_t)x->n * x->h * x->w * 2;
+    const bool fits = x->w % 32 == 0 && x->c % 32 == 0 && dy->c % 32 == 0 && workspace &&
+                      workspace_bytes >= need && (reinterpret_cast<uintptr_t>(workspace) & 255) == 0;
+    if (engine == 1 && !fits)
+        return fail(STENCIL_EINVAL, "tcgen05 weight gradient needs W %% 32 == 0 and a %zu-byte workspace", need);
+    if (engine == 0) engine = fits ? 1 : 2;
+    if (engine == 1) {
+        const int cin = x->c;
+        int rc = cin % 128 == 0 ? launch_wgrad_tma<128>(x, dy, dw, dilation, workspace, STREAM(s))
+                 : cin % 64 == 0 ? launch_wgrad_tma<64>(x, dy, dw, dilation, workspace, STREAM(s))
+                                 : launch_wgrad_tma<32>(x, dy, dw, dilation, workspace, STREAM(s));
+        if (rc || !db) return rc;
+        const long long P = (long long)x->n * x->h * x->w;
+        dim3 g2((unsigned)std::min<long long>(1024, (P + 255) / 256), (dy->c + 31) / 32);
+        k_bias_grad<<<g2, 256, 0, STREAM(s)>>>(to_act(*dy), db);
+        return cuda_fail(cudaGetLastError(), "bias grad launch");
+    }
+    return unet_conv3x3_wgrad_dil(x, dy, dw, db, dilation, s);
 }
 
 extern "C" int unet_conv3x3_wgrad_dil(const unet_act *x, const unet_act *dy, float *dw, float *db,

@@ -61,6 +61,8 @@ def _L():
             "unet_conv3x3_fwd_dil": [A, vp, vp, A, i, i, vp],
             "unet_conv3x3_fwd_engine": [A, vp, vp, A, i, i, i, vp],
             "unet_conv3x3_wgrad_dil": [A, A, vp, vp, i, vp],
+            "unet_conv3x3_wgrad_engine": [A, A, vp, vp, i, i, vp, ctypes.c_size_t, vp],
+            "unet_wgrad_workspace_bytes": [A, A, ctypes.POINTER(ctypes.c_size_t)],
             "unet_flip_weights": [vp, vp, i, i, vp],
             "unet_conv3x3_wgrad": [A, A, vp, vp, vp],
             "unet_relu_bwd": [A, A, vp],
@@ -256,13 +258,27 @@ class UNet:
         P = self.params[name]
         _chk(L.unet_relu_bwd(ctypes.byref(gy), ctypes.byref(y), s), "relu_bwd " + name)
         d = DILATION.get(name, 1)
-        _chk(L.unet_conv3x3_wgrad_dil(ctypes.byref(x), ctypes.byref(gy), _p(P["dw"]), _p(P["db"]), d, s),
+        ws = self._wgrad_ws(x, gy)
+        _chk(L.unet_conv3x3_wgrad_engine(ctypes.byref(x), ctypes.byref(gy), _p(P["dw"]), _p(P["db"]), d, 0,
+                                         _p(ws), ws.numel(), s),
              "wgrad " + name)
         if gx is not None:
             cin, cout = P["w"].shape[2], P["w"].shape[0]
             _chk(L.unet_flip_weights(_p(P["wb"]), _p(P["wt"]), cout, cin, s), "flip " + name)
             _chk(L.unet_conv3x3_fwd_dil(ctypes.byref(gy), _p(P["wt"]), None, ctypes.byref(gx), 0, d, s),
                  "dgrad " + name)
+
+    def _wgrad_ws(self, x, gy):
+        """Device workspace for the tcgen05 weight gradient (channel-major
+        copies of the layer's input and output gradient), grown on demand."""
+        import torch
+        need = ctypes.c_size_t()
+        _chk(_L().unet_wgrad_workspace_bytes(ctypes.byref(x), ctypes.byref(gy), ctypes.byref(need)),
+             "wgrad workspace")
+        ws = getattr(self, "_ws", None)
+        if ws is None or ws.numel() < need.value:
+            self._ws = ws = torch.empty(need.value, dtype=torch.uint8, device=self.device)
+        return ws
 
     def zero_grad(self):
         for name, _, _ in LAYERS:
