@@ -107,8 +107,8 @@ def test_library_beats_reference_kernels_512(cuda, radius):
 def test_library_beats_reference_kernels_2d_256(cuda):
     """2-D 256^2 R=1, 1000 sweeps (the reference's 2-D configuration), LEGACY
     from the reference's initial state: every reference kernel x block shape
-    built for it against the library's AUTO engine (one cluster launch),
-    bit for bit and in time."""
+    built for it against the library's AUTO engine (one cooperative launch of
+    the temporally blocked 2-D kernel), bit for bit and in time."""
     import torch
     from thesis_gb300 import lib, stencil as S
     cfgs = [c for c in OB.REF_GPU_CONFIGS if c[0] == 2 and c[1] == 256]

@@ -8,7 +8,7 @@ Here every candidate runs in-process through the C ABI:
     with 32 <= bx*by*bz <= 1024 and bx >= by >= bz, bx >= 8,
     Autotuning/tuner/optimisation.py:150-160; coarsening factors; radius and
     size from the workload), extended with this library's variants, stream
-    tile shapes and cluster sizes;
+    tile shapes, cluster sizes and the 2-D temporal blocking depth and tile;
   * the optimiser is a two-level variable tree, as the reference's
     independence tree (Autotuning/tuner/vartree.py): the variant is chosen
     first, each with its default parameters, then the winner's own
@@ -67,6 +67,13 @@ def variant_space(shape, radius):
         if radius <= 4:
             top.append({"variant": "cluster"})
             sub["cluster"] = {}
+        if dims == 2 and radius <= 4:
+            # temporally blocked cooperative engine: sweeps per exchange and
+            # the tile (block_x * coarsen_x by block_y cells)
+            top.append({"variant": "coop"})
+            sub["coop"] = {"temporal": [0, 2, 4, 6, 8, 10, 12, 16, 20],
+                           "block": [(0, 0, 1), (16, 16, 1), (24, 20, 1), (32, 16, 1),
+                                     (16, 32, 1), (32, 32, 1), (24, 24, 1)]}
     return top, sub
 
 

@@ -217,9 +217,11 @@ static bool tuned_choice(const stencil_params &p, stencil_params *out) {
     return false;
 }
 
-// Variant choice when the caller leaves it to the library: grids that fit a
-// cluster's shared memory run all sweeps in one cluster launch (launch- and
-// sync-bound otherwise); large 3-D grids stream; the rest use the base kernel.
+// Variant choice when the caller leaves it to the library: 2-D grids small
+// enough for one tile per SM run the temporally blocked cooperative engine;
+// other grids that fit a cluster's shared memory run all sweeps in one
+// cluster launch (launch- and sync-bound otherwise); large 3-D grids stream;
+// the rest use the base kernel.
 void note_launches(const char *engine, long long n) {
     if (!t_launches) t_engine = engine;
     t_launches += n;
@@ -227,6 +229,8 @@ void note_launches(const char *engine, long long n) {
 
 static int choose_variant(const stencil_params &p) {
     const Geom g = make_geom(p);
+    // small 2-D grids: every SM, temporally blocked (2-5x the one-cluster engine)
+    if (p.dims == 2 && p.iterations >= 8 && tb2d_supported(g, 2)) return STENCIL_VARIANT_COOP;
     if (p.iterations >= 8 && cluster_resident(g, p.dims)) return STENCIL_VARIANT_CLUSTER;
     if (p.dims == 3 && stream3d_supported(g)) return STENCIL_VARIANT_SMEM_REGISTER;
     return STENCIL_VARIANT_BASE;
@@ -307,6 +311,16 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
     if ((variant == STENCIL_VARIANT_SMEM || variant == STENCIL_VARIANT_SMEM_PADDED) &&
         !tile_supported(g, p->dims))
         variant = STENCIL_VARIANT_BASE;
+    if (variant == STENCIL_VARIANT_COOP && p->dims == 2 && tb2d_supported(g, 2)) {
+        // Whole GPU, one tile per SM, `temporal` sweeps per exchange; the
+        // tile is block_x * coarsen_x by block_y cells when given.
+        float *res = nullptr;
+        rc = run_tb2d(g, cur, nxt, p->iterations, p->temporal,
+                      p->block_x * std::max(p->coarsen_x, 1), p->block_y, s, &res);
+        if (rc) return rc;
+        if (d_result) *d_result = res;
+        return STENCIL_OK;
+    }
     if (variant == STENCIL_VARIANT_COOP && cluster_resident(g, p->dims))
         variant = STENCIL_VARIANT_CLUSTER;
     if (variant == STENCIL_VARIANT_CLUSTER) {
@@ -522,6 +536,7 @@ int stencil_device_status(int *status) {
 }
 
 int stencil_release(void) {
+    tb2d_release();
     std::lock_guard<std::mutex> lock(g_ws_mu);
     const int dev = current_device();
     if (dev < 0 || dev >= 64) return STENCIL_OK;

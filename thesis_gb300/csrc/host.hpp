@@ -56,6 +56,17 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
                  cudaStream_t s, float **res, int shape_hint = 0, bool persistent = false);
 int run_tb3d(const Geom &g, float *a, float *b, int iters, int temporal, cudaStream_t s,
              float **res);
+// A zeroed grid-barrier counter for one persistent launch on stream s
+// (round-robin over a fixed device array; k_stream.cu).
+int grid_bar_slot(cudaStream_t s, unsigned **slot);
+// Small 2-D grids: all sweeps in one cooperative launch, one tile per CTA,
+// `temporal` sweeps per exchange through global memory (k_tb2d.cu).
+// tile_x/tile_y/temporal 0 = chosen by the library.  tb2d_release frees the
+// current device's exchange buffers.
+bool tb2d_supported(const Geom &g, int dims);
+int run_tb2d(const Geom &g, float *a, float *b, int iters, int temporal, int tile_x, int tile_y,
+             cudaStream_t s, float **res);
+void tb2d_release();
 // All sweeps of one grid on one thread-block cluster (k_cluster.cu).
 int run_cluster(const Geom &g, int dims, float *a, float *b, int iters, cudaStream_t s,
                 float **res);

@@ -371,6 +371,8 @@ StreamKernel pick(int r, int shape) {
     }
 }
 
+}  // namespace
+
 // Grid-barrier counters of the persistent launches: a fixed device array (no
 // allocation, so a launch can be captured in a CUDA graph), one slot per
 // launch taken round-robin and zeroed on the launch's stream just before it.
@@ -385,6 +387,8 @@ int grid_bar_slot(cudaStream_t s, unsigned **slot) {
     ST_CUDA(cudaMemsetAsync(*slot, 0, sizeof(unsigned), s));
     return STENCIL_OK;
 }
+
+namespace {
 
 // Sets the kernel's shared-memory limit and returns its resident CTAs per SM,
 // once per kernel and device (later calls, e.g. inside a CUDA graph capture,
