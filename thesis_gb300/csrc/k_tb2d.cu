@@ -48,6 +48,7 @@ namespace {
 constexpr int kTb2Threads = 512;
 constexpr int kTb2MaxItems = 4;  // float4 chunks of the extended tile per thread
 constexpr int kTb2RingUnroll = 4;  // halo pairs a thread requests at once
+constexpr int kTb2MaxT = 32;       // sweeps per exchange (and s_region entries)
 constexpr int kTb2SmemMax = 160 * 1024;
 constexpr int kTb2MaxTiles = 256;
 
@@ -103,7 +104,9 @@ __device__ __forceinline__ float4 tb2_chunk(const float *c, int pw) {
     return make_float4(out[0], out[1], out[2], out[3]);
 }
 
-template <int R, bool LEGACY>
+// NI: chunks of the extended tile per thread (1, 2 or 4: the smallest that
+// covers it; every unused slot costs latency in each sweep).
+template <int R, bool LEGACY, int NI>
 __global__ void __launch_bounds__(kTb2Threads, 1)
     k_tb2d(float *g0, float *g1, Geom g, Tb2Plan p, int iters, unsigned long long *xch) {
     extern __shared__ __align__(16) float tb2_smem[];
@@ -119,6 +122,39 @@ __global__ void __launch_bounds__(kTb2Threads, 1)
     // The extended tile clipped to the grid.
     const int exa = max(ox, 0), exb = min(ox + pw, nx);
     const int eya = max(oy, 0), eyb = min(oy + p.ph, ny);
+
+    // This thread's float4 chunks of the extended tile, fixed for the launch
+    // (chunk column, row, shared-memory offset; -1: none), so a sweep costs
+    // no index arithmetic: only a compare with the sweep's region.
+    const int nc = pw >> 2;
+    int icol[NI], irow[NI], ioff[NI];
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+        const int u = threadIdx.x + i * kTb2Threads;
+        icol[i] = irow[i] = -1;
+        if (u < nc * p.ph) {
+            icol[i] = u % nc;
+            irow[i] = u / nc;
+        }
+        ioff[i] = irow[i] * pw + 4 * icol[i];
+    }
+    // Region of each sweep of a block in local chunk columns [x, y) and rows
+    // [z, w): the owned tile grown by (kk - k) * R, inside the update region;
+    // a chunk's cells outside it are computed from whatever the tile holds
+    // there and never read before being recomputed; border cells are never
+    // written.  Written by threads 0..kk-1 while the previous block ends.
+    __shared__ int4 s_region[kTb2MaxT];
+    auto plan_block = [&](int kk) {
+        if (threadIdx.x < kk) {
+            const int ext = (kk - 1 - threadIdx.x) * R;
+            const int rxa = max(x0 - ext, R), rxb = min(x1 + ext, nx - R);
+            const int rya = max(y0 - ext, R), ryb = min(y1 + ext, ny - R);
+            int4 b = make_int4(0, 0, 0, 0);
+            if (rxa < rxb && rya < ryb)
+                b = make_int4((rxa - ox) >> 2, (rxb - ox + 3) >> 2, rya - oy, ryb - oy);
+            s_region[threadIdx.x] = b;
+        }
+    };
 
     // Initial state: the first buffer's extended tile, the second buffer's
     // border band (its interior is rewritten by the first sweep before any read).
@@ -139,33 +175,23 @@ __global__ void __launch_bounds__(kTb2Threads, 1)
             }
         }
     }
+    int kk = min(T, iters);
+    plan_block(kk);
     __syncthreads();
 
     int cur = 0;  // shared buffer holding the newest state
     unsigned blk = 0;
     for (int done = 0; done < iters;) {
-        const int kk = min(T, iters - done);
         for (int k = 1; k <= kk; ++k) {
             const float *src = cur ? S1 : S0;
             float *dst = cur ? S0 : S1;
-            // sweep k's region (the owned tile grown by (kk - k) * R, inside
-            // the update region), in whole chunks: a chunk's extra cells are
-            // computed from whatever the tile holds there and never read
-            // before being recomputed; border cells are never written
-            const int ext = (kk - k) * R;
-            const int rxa = max(x0 - ext, R), rxb = min(x1 + ext, nx - R);
-            const int rya = max(y0 - ext, R), ryb = min(y1 + ext, ny - R);
-            const int cxa = rxa & ~3, nch = (((rxb + 3) & ~3) - cxa) >> 2;
-            const int n = nch * max(ryb - rya, 0);
-            const float inv = 1.0f / (float)nch;
-            for (int j = threadIdx.x; j < n; j += kTb2Threads) {
-                // j / nch exactly: (j + 0.5) / nch is at least 0.5 / nch from
-                // an integer, far above the float error for j < 2^20
-                const int row = (int)(((float)j + 0.5f) * inv);
-                const int gx = cxa + 4 * (j - row * nch), gy = rya + row;
-                const int si = (gy - oy) * pw + (gx - ox);
-                const float4 v = tb2_chunk<R, LEGACY>(src + si, pw);
-                float *q = dst + si;
+            const int4 rg = s_region[k - 1];
+#pragma unroll
+            for (int i = 0; i < NI; ++i) {
+                if (icol[i] < rg.x || icol[i] >= rg.y || irow[i] < rg.z || irow[i] >= rg.w) continue;
+                const float4 v = tb2_chunk<R, LEGACY>(src + ioff[i], pw);
+                float *q = dst + ioff[i];
+                const int gx = ox + 4 * icol[i];
                 if (gx >= R && gx + 3 < nx - R) {
                     *reinterpret_cast<float4 *>(q) = v;
                 } else {
@@ -198,6 +224,8 @@ __global__ void __launch_bounds__(kTb2Threads, 1)
                              : "memory");
             }
         }
+        kk = min(T, iters - done);
+        plan_block(kk);
         // Read the halo ring from the neighbours' tiles, waiting for block
         // blk: every pair of a thread is requested before any is checked, so
         // the common case costs one L2 round trip.
@@ -289,14 +317,26 @@ __global__ void __launch_bounds__(kTb2Threads, 1)
 
 using Tb2Fn = void (*)(float *, float *, Geom, Tb2Plan, int, unsigned long long *);
 
-Tb2Fn tb2_fn(int r, bool legacy) {
+template <int R, bool LEGACY>
+Tb2Fn tb2_fn_ni(int ni) {
+    return ni <= 1 ? k_tb2d<R, LEGACY, 1> : ni <= 2 ? k_tb2d<R, LEGACY, 2> : k_tb2d<R, LEGACY, 4>;
+}
+
+// The kernel for radius r, mode and chunks per thread (1, 2 or 4).
+Tb2Fn tb2_fn(int r, bool legacy, int ni) {
     switch (r) {
-        case 1: return legacy ? k_tb2d<1, true> : k_tb2d<1, false>;
-        case 2: return legacy ? k_tb2d<2, true> : k_tb2d<2, false>;
-        case 3: return legacy ? k_tb2d<3, true> : k_tb2d<3, false>;
-        case 4: return legacy ? k_tb2d<4, true> : k_tb2d<4, false>;
+        case 1: return legacy ? tb2_fn_ni<1, true>(ni) : tb2_fn_ni<1, false>(ni);
+        case 2: return legacy ? tb2_fn_ni<2, true>(ni) : tb2_fn_ni<2, false>(ni);
+        case 3: return legacy ? tb2_fn_ni<3, true>(ni) : tb2_fn_ni<3, false>(ni);
+        case 4: return legacy ? tb2_fn_ni<4, true>(ni) : tb2_fn_ni<4, false>(ni);
         default: return nullptr;
     }
+}
+
+// Chunks per thread a plan needs.
+int plan_items(const Tb2Plan &p) {
+    const int n = (p.pw / 4) * p.ph;
+    return n <= kTb2Threads ? 1 : n <= 2 * kTb2Threads ? 2 : 4;
 }
 
 int roundup4(int v) { return (v + 3) & ~3; }
@@ -327,9 +367,11 @@ bool make_plan(const Geom &g, int t, int tx, int ty, int max_ctas, Tb2Plan *p) {
 
 // Modelled time per sweep, in SM cycles, fitted to clock64 timings of the
 // kernel's phases on a GB300 (256^2, R = 1): a block costs its exchange
-// (about 2500 cycles of L2 latency plus 1.4 per halo pair read) and, per
-// sweep, about 450 cycles of barrier-bound latency plus 0.6 per float4 chunk
-// of the sweep's region (more for larger radii: more loads per chunk).
+// (about 2500 cycles of L2 latency plus 1.4 per halo pair read) and each
+// sweep about 300 cycles of latency (shared-memory loads, the CTA barrier),
+// 50 per chunk slot of a thread, and the shared-memory wavefronts of its
+// region (3 + 2R loads and one store of 16 bytes per chunk, a quarter-warp
+// each).
 double plan_cost(const Geom &g, const Tb2Plan &p) {
     const int R = g.radius;
     const long long ring = ((long long)p.pw * p.ph - (long long)p.tx * p.ty) / 2;
@@ -337,7 +379,7 @@ double plan_cost(const Geom &g, const Tb2Plan &p) {
     for (int k = 1; k <= p.t; ++k) {
         const int ext = (p.t - k) * R;
         const int chunks = (p.tx + 2 * roundup4(ext)) / 4, rows = p.ty + 2 * ext;
-        c += 450.0 + (0.4 + 0.2 * R) * chunks * rows;
+        c += 300.0 + 50.0 * plan_items(p) + (0.5 + 0.25 * R) * chunks * rows;
     }
     return c / p.t;
 }
@@ -444,18 +486,19 @@ int tb2_max_ctas(int r) {
     for (auto &c : cache)
         if (c.first == dev * 8 + r) return c.second;
     int n = 1 << 30;
-    for (bool legacy : {false, true}) {
-        const void *fn = reinterpret_cast<const void *>(tb2_fn(r, legacy));
-        int m = 0;
-        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kTb2SmemMax) !=
-                cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, fn, kTb2Threads, kTb2SmemMax) !=
-                cudaSuccess) {
-            cudaGetLastError();
-            m = 0;
+    for (bool legacy : {false, true})
+        for (int ni : {1, 2, 4}) {
+            const void *fn = reinterpret_cast<const void *>(tb2_fn(r, legacy, ni));
+            int m = 0;
+            if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kTb2SmemMax) !=
+                    cudaSuccess ||
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, fn, kTb2Threads, kTb2SmemMax) !=
+                    cudaSuccess) {
+                cudaGetLastError();
+                m = 0;
+            }
+            n = std::min(n, m);
         }
-        n = std::min(n, m);
-    }
     const int ctas = n >= 1 ? std::min(num_sms(), kTb2MaxTiles) : 0;
     cache.push_back({dev * 8 + r, ctas});
     return ctas;
@@ -493,7 +536,7 @@ int run_tb2d(const Geom &g, float *a, float *b, int iters, int temporal, int til
         return fail(STENCIL_EUNSUPPORTED, "grid too large for one tile per SM");
     if (res) *res = (iters & 1) ? b : a;
     if (iters <= 0) return STENCIL_OK;
-    const void *fn = reinterpret_cast<const void *>(tb2_fn(g.radius, g.legacy != 0));
+    const void *fn = reinterpret_cast<const void *>(tb2_fn(g.radius, g.legacy != 0, plan_items(p)));
     const int grid = p.tiles_x * p.tiles_y;
     const size_t smem = 2ull * p.pw * p.ph * sizeof(float);
     unsigned long long *xch = nullptr;
