@@ -47,7 +47,6 @@ namespace {
 
 constexpr int kTb2Threads = 512;
 constexpr int kTb2MaxItems = 4;  // float4 chunks of the extended tile per thread
-constexpr int kTb2RingUnroll = 4;  // halo pairs a thread requests at once
 constexpr int kTb2MaxT = 32;       // sweeps per exchange (and s_region entries)
 constexpr int kTb2SmemMax = 160 * 1024;
 constexpr int kTb2MaxTiles = 256;
@@ -155,6 +154,35 @@ __global__ void __launch_bounds__(kTb2Threads, 1)
             s_region[threadIdx.x] = b;
         }
     };
+    // This thread's exchange pairs, fixed for the launch (the extended tile
+    // holds at most 2 * NI * kTb2Threads pairs of cells): own pairs to publish
+    // (shared-memory offset, word offset in the exchange slot; -1: none) and
+    // halo pairs to read (word offset in the slot, shared-memory offset).
+    constexpr int NP = 2 * NI;
+    int pub_s[NP], pub_w[NP], ring_w[NP], ring_s[NP];
+    {
+        const int ocw = (x1 - x0) >> 1, on = ocw * (y1 - y0);
+        const int ecw = (exb - exa) >> 1, en = ecw * (eyb - eya);
+#pragma unroll
+        for (int i = 0; i < NP; ++i) {
+            const int u = threadIdx.x + i * kTb2Threads;
+            pub_s[i] = pub_w[i] = ring_w[i] = ring_s[i] = -1;
+            if (u < on) {
+                const int y = y0 + u / ocw, x = x0 + 2 * (u % ocw);
+                pub_s[i] = (y - oy) * pw + (x - ox);
+                pub_w[i] = (int)(tile * tile_words) + (y - y0) * p.tx + (x - x0);
+            }
+            if (u < en) {
+                const int y = eya + u / ecw, x = exa + 2 * (u % ecw);
+                if (!(x >= x0 && x < x1 && y >= y0 && y < y1)) {  // not an own cell
+                    const int ocx = x / p.tx, ocy = y / p.ty;
+                    ring_w[i] = (int)((ocy * p.tiles_x + ocx) * tile_words) + (y - ocy * p.ty) * p.tx +
+                                (x - ocx * p.tx);
+                    ring_s[i] = (y - oy) * pw + (x - ox);
+                }
+            }
+        }
+    }
 
     // Initial state: the first buffer's extended tile, the second buffer's
     // border band (its interior is rewritten by the first sweep before any read).
@@ -209,20 +237,15 @@ __global__ void __launch_bounds__(kTb2Threads, 1)
         if (done >= iters) break;
         const float *S = cur ? S1 : S0;
         float *Sw = cur ? S1 : S0;
+        unsigned long long *slot = xch + (size_t)(blk & 1) * ntiles * tile_words;
         // Publish the owned tile (pairs of cells; tx and x0 are multiples of 4).
-        {
-            unsigned long long *mine = xch + ((size_t)(blk & 1) * ntiles + tile) * tile_words;
-            const int cw = (x1 - x0) >> 1;
-            const int n = cw * (y1 - y0);
-            for (int u = threadIdx.x; u < n; u += kTb2Threads) {
-                const int y = y0 + u / cw, x = x0 + 2 * (u % cw);
-                const float2 v = *reinterpret_cast<const float2 *>(S + (y - oy) * pw + (x - ox));
-                const unsigned long long a = tb2_word(v.x, blk), b = tb2_word(v.y, blk);
-                asm volatile("st.volatile.global.v2.u64 [%0], {%1, %2};" ::"l"(
-                                 mine + (size_t)(y - y0) * p.tx + (x - x0)),
-                             "l"(a), "l"(b)
-                             : "memory");
-            }
+#pragma unroll
+        for (int i = 0; i < NP; ++i) {
+            if (pub_s[i] < 0) continue;
+            const float2 v = *reinterpret_cast<const float2 *>(S + pub_s[i]);
+            asm volatile("st.volatile.global.v2.u64 [%0], {%1, %2};" ::"l"(slot + pub_w[i]),
+                         "l"(tb2_word(v.x, blk)), "l"(tb2_word(v.y, blk))
+                         : "memory");
         }
         kk = min(T, iters - done);
         plan_block(kk);
@@ -231,56 +254,34 @@ __global__ void __launch_bounds__(kTb2Threads, 1)
         // the common case costs one L2 round trip.
         bool ok = true;
         {
-            const int cw = (exb - exa) >> 1;
-            const int n = cw * (eyb - eya);
-            for (int u0 = 0; u0 < n && ok; u0 += kTb2RingUnroll * kTb2Threads) {
-                const unsigned long long *srcp[kTb2RingUnroll];
-                int dsti[kTb2RingUnroll];
-                unsigned long long a[kTb2RingUnroll], b[kTb2RingUnroll];
+            unsigned long long a[NP], b[NP];
 #pragma unroll
-                for (int i = 0; i < kTb2RingUnroll; ++i) {
-                    const int u = u0 + threadIdx.x + i * kTb2Threads;
-                    srcp[i] = nullptr;
-                    dsti[i] = 0;
-                    if (u < n) {
-                        const int y = eya + u / cw, x = exa + 2 * (u % cw);
-                        if (!(x >= x0 && x < x1 && y >= y0 && y < y1)) {  // not an own cell
-                            const int ocx = x / p.tx, ocy = y / p.ty;
-                            srcp[i] = xch +
-                                      ((size_t)(blk & 1) * ntiles + ocy * p.tiles_x + ocx) * tile_words +
-                                      (size_t)(y - ocy * p.ty) * p.tx + (x - ocx * p.tx);
-                            dsti[i] = (y - oy) * pw + (x - ox);
-                        }
+            for (int i = 0; i < NP; ++i) {
+                a[i] = b[i] = 0;
+                if (ring_w[i] >= 0)
+                    asm volatile("ld.volatile.global.v2.u64 {%0, %1}, [%2];"
+                                 : "=l"(a[i]), "=l"(b[i])
+                                 : "l"(slot + ring_w[i])
+                                 : "memory");
+            }
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                if (ring_w[i] < 0) continue;
+                uint64_t t0 = 0;
+                while (ok && ((unsigned)(a[i] >> 32) != blk || (unsigned)(b[i] >> 32) != blk)) {
+                    const uint64_t t = globaltimer_ns();
+                    if (!t0) t0 = t;
+                    else if (t - t0 > kWaitLimitNs) {
+                        report_status(kStatusTimeout);
+                        ok = false;
                     }
+                    asm volatile("ld.volatile.global.v2.u64 {%0, %1}, [%2];"
+                                 : "=l"(a[i]), "=l"(b[i])
+                                 : "l"(slot + ring_w[i])
+                                 : "memory");
                 }
-#pragma unroll
-                for (int i = 0; i < kTb2RingUnroll; ++i) {
-                    a[i] = b[i] = 0;
-                    if (srcp[i])
-                        asm volatile("ld.volatile.global.v2.u64 {%0, %1}, [%2];"
-                                     : "=l"(a[i]), "=l"(b[i])
-                                     : "l"(srcp[i])
-                                     : "memory");
-                }
-#pragma unroll
-                for (int i = 0; i < kTb2RingUnroll; ++i) {
-                    if (!srcp[i]) continue;
-                    uint64_t t0 = 0;
-                    while (ok && ((unsigned)(a[i] >> 32) != blk || (unsigned)(b[i] >> 32) != blk)) {
-                        const uint64_t t = globaltimer_ns();
-                        if (!t0) t0 = t;
-                        else if (t - t0 > kWaitLimitNs) {
-                            report_status(kStatusTimeout);
-                            ok = false;
-                        }
-                        asm volatile("ld.volatile.global.v2.u64 {%0, %1}, [%2];"
-                                     : "=l"(a[i]), "=l"(b[i])
-                                     : "l"(srcp[i])
-                                     : "memory");
-                    }
-                    *reinterpret_cast<float2 *>(Sw + dsti[i]) =
-                        make_float2(__uint_as_float((unsigned)a[i]), __uint_as_float((unsigned)b[i]));
-                }
+                *reinterpret_cast<float2 *>(Sw + ring_s[i]) =
+                    make_float2(__uint_as_float((unsigned)a[i]), __uint_as_float((unsigned)b[i]));
             }
         }
         if (!__syncthreads_and(ok)) return;

@@ -46,12 +46,12 @@ def main(case):
         for _ in range(4):
             S.sweep(a, b, 1, 1000, J, "cluster")
     elif case == "tb2d_256":
-        # the 2-D temporally blocked engine on 256^2, 1000 sweeps per launch
-        # (24 x 20 tiles, 12 sweeps per exchange)
+        # the 2-D temporally blocked engine AUTO runs on 256^2, 1000 sweeps
+        # per launch
         u = S.init_uniform((256, 256), 1)
         a, b = u.clone(), u.clone()
         for _ in range(4):
-            S.sweep(a, b, 1, 1000, J, "coop", block=(24, 20, 0), temporal=12)
+            S.sweep(a, b, 1, 1000, J, "auto")
     elif case == "lp_sweep_r4":
         u = S.init_fourier((384, 384, 384), 1, 4)
         for _ in range(2):
