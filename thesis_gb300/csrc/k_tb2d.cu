@@ -367,20 +367,20 @@ bool make_plan(const Geom &g, int t, int tx, int ty, int max_ctas, Tb2Plan *p) {
 }
 
 // Modelled time per sweep, in SM cycles, fitted to clock64 timings of the
-// kernel's phases on a GB300 (256^2, R = 1): a block costs its exchange
-// (about 2500 cycles of L2 latency plus 1.4 per halo pair read) and each
-// sweep about 300 cycles of latency (shared-memory loads, the CTA barrier),
-// 50 per chunk slot of a thread, and the shared-memory wavefronts of its
-// region (3 + 2R loads and one store of 16 bytes per chunk, a quarter-warp
-// each).
+// kernel's phases on a GB300 (64^2 to 512^2, R = 1): a block costs its
+// exchange (about 1800 cycles of L2 latency, 1.35 per halo pair read and 400
+// per further pair slot of a thread) and each sweep about 350 cycles of
+// latency (shared-memory loads, the CTA barrier), 90 per further chunk slot
+// of a thread, and the shared-memory traffic of its region (3 + 2R loads and
+// one store of 16 bytes per chunk).
 double plan_cost(const Geom &g, const Tb2Plan &p) {
-    const int R = g.radius;
+    const int R = g.radius, ni = plan_items(p);
     const long long ring = ((long long)p.pw * p.ph - (long long)p.tx * p.ty) / 2;
-    double c = 2500.0 + 1.4 * ring;
+    double c = 1800.0 + 1.35 * ring + 400.0 * (ni - 1);
     for (int k = 1; k <= p.t; ++k) {
         const int ext = (p.t - k) * R;
         const int chunks = (p.tx + 2 * roundup4(ext)) / 4, rows = p.ty + 2 * ext;
-        c += 300.0 + 50.0 * plan_items(p) + (0.5 + 0.25 * R) * chunks * rows;
+        c += 350.0 + 90.0 * (ni - 1) + (0.4 + 0.15 * R) * chunks * rows;
     }
     return c / p.t;
 }
