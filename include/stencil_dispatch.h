@@ -64,7 +64,11 @@ enum {
     STENCIL_VARIANT_SMEM = 2,          /* TMA-staged shared-memory tile with halo */
     STENCIL_VARIANT_SMEM_PADDED = 3,   /* same kernel as SMEM */
     STENCIL_VARIANT_SMEM_REGISTER = 4, /* 2.5D stream along the slowest axis */
-    STENCIL_VARIANT_COOP = 5,          /* temporally blocked: several sweeps per HBM pass */
+    STENCIL_VARIANT_COOP = 5,          /* all sweeps in one cooperative launch; 3-D: one
+                                          sweep (temporal 1) or several per HBM pass;
+                                          2-D grids of at most one tile per SM: every SM,
+                                          `temporal` sweeps per halo exchange, tile
+                                          block_x * coarsen_x by block_y cells (0: chosen) */
     STENCIL_VARIANT_CLUSTER = 6        /* whole grid resident in a thread-block cluster */
 };
 
@@ -78,7 +82,7 @@ typedef struct stencil_params {
     int variant;     /* STENCIL_VARIANT_* */
     int block_x, block_y, block_z; /* thread-block shape hint */
     int coarsen_x;   /* cells per thread along x (vector kernels use multiples of 4) */
-    int temporal;    /* sweeps per pass for STENCIL_VARIANT_COOP */
+    int temporal;    /* sweeps per pass (3-D) or per exchange (2-D) for STENCIL_VARIANT_COOP */
     int reserved[4]; /* must be zero */
 } stencil_params;
 
@@ -96,8 +100,12 @@ STENCIL_API int stencil_params_check(const stencil_params *p);
  *         ping-pong scratch)
  *   d_u2  device buffer of the same size (ping-pong scratch; its border band
  *         is read, never written)
- * Runs asynchronously on `stream`, allocates nothing, and writes to *d_result
- * (if non-NULL) which of d_u1 / d_u2 holds the state after the last sweep.
+ * Runs asynchronously on `stream` and writes to *d_result (if non-NULL) which
+ * of d_u1 / d_u2 holds the state after the last sweep.  Allocates nothing,
+ * except that the 2-D temporally blocked engine (COOP or AUTO on small 2-D
+ * grids) keeps a per-device exchange buffer, grown on first use (outside a
+ * CUDA graph capture: run such a dispatch once before capturing it) and freed
+ * by stencil_release().
  * Both buffers must be 16-byte aligned (cudaMalloc gives 256). */
 STENCIL_API int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
                         stencil_stream_t stream, float **d_result);
@@ -162,11 +170,18 @@ STENCIL_API int stencil_batch_workspace_bytes(int njobs, size_t *bytes);
 STENCIL_API int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, int cluster_size,
                                       void *d_workspace, size_t workspace_bytes,
                                       stencil_stream_t stream);
-/* One persistent launch over the prepared jobs: resets the queue counter and
- * launches every cluster the device can hold.  Asynchronous; allocates
- * nothing; can be captured into a CUDA graph (the queue reset is a memset
- * node, so every replay runs the whole batch again). */
+/* Runs the prepared jobs: one persistent cluster launch over a device work
+ * queue (every cluster the device can hold) for the jobs that a cluster
+ * sweeps, then, for each 3-D job too large for a cluster's shared memory,
+ * one persistent whole-GPU launch.  Resets the queue counter first.
+ * Asynchronous; allocates nothing; can be captured into a CUDA graph (the
+ * queue reset is a memset node, so every replay runs the whole batch
+ * again). */
 STENCIL_API int stencil_batch_launch(const void *d_workspace, stencil_stream_t stream);
+/* How stencil_batch_launch runs a prepared workspace: *cluster_jobs jobs in
+ * the cluster launch (none: no cluster launch), *whole_gpu_jobs jobs with a
+ * launch of their own. */
+STENCIL_API int stencil_batch_plan(const void *d_workspace, int *cluster_jobs, int *whole_gpu_jobs);
 /* Drops the host-side record of a prepared workspace (call before freeing it). */
 STENCIL_API int stencil_batch_forget(const void *d_workspace);
 

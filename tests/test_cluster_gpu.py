@@ -114,4 +114,10 @@ def test_batch_matches_oracle_and_graph_replay(cuda, cluster_size):
     torch.cuda.synchronize()
     for k in range(len(specs)):
         assert bits_equal(b.result(k).cpu().numpy(), wants[k]), k
+    # every job runs once: in the cluster launch or in a whole-GPU launch of
+    # its own (3-D grids too large for a cluster's shared memory)
+    c, w = b.plan()
+    assert c + w == len(specs)
+    assert w >= sum(1 for shape, _, _ in specs if len(shape) == 3 and shape[0] >= 96)
+    assert b.kernel_launches() == (1 if c else 0) + w
     b.close()

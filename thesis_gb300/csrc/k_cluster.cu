@@ -658,6 +658,16 @@ extern "C" int stencil_batch_launch(const void *d_workspace, stencil_stream_t st
     return STENCIL_OK;
 }
 
+extern "C" int stencil_batch_plan(const void *d_workspace, int *cluster_jobs, int *whole_gpu_jobs) {
+    if (!d_workspace || !cluster_jobs || !whole_gpu_jobs) return fail(STENCIL_EINVAL, "null argument");
+    BatchPlan plan;
+    if (!recall(d_workspace, &plan))
+        return fail(STENCIL_EINVAL, "workspace was not prepared by stencil_batch_prepare");
+    *cluster_jobs = plan.h.njobs;
+    *whole_gpu_jobs = (int)plan.streamed.size();
+    return STENCIL_OK;
+}
+
 extern "C" int stencil_batch_forget(const void *d_workspace) {
     std::lock_guard<std::mutex> lock(g_batch_mu);
     for (size_t i = 0; i < g_batch.size(); ++i)

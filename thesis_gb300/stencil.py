@@ -232,6 +232,18 @@ class Batch:
         _lib.check(_lib.load().stencil_batch_launch(self.ws, _stream_handle(stream)),
                    "stencil_batch_launch")
 
+    def plan(self):
+        """(jobs in the cluster launch, jobs with a whole-GPU launch of their own)."""
+        c, w = ctypes.c_int(), ctypes.c_int()
+        _lib.check(_lib.load().stencil_batch_plan(self.ws, ctypes.byref(c), ctypes.byref(w)),
+                   "stencil_batch_plan")
+        return c.value, w.value
+
+    def kernel_launches(self):
+        """Kernel launches of one ``launch`` (one replay of its CUDA graph)."""
+        c, w = self.plan()
+        return (1 if c else 0) + w
+
     def result(self, k):
         u1, u2, _, iters, _ = self.jobs[k]
         return u1 if iters % 2 == 0 else u2
