@@ -191,8 +191,8 @@ STENCIL_API int stencil_batch_forget(const void *d_workspace);
  * d_u, the correction e of (I - M) e = r is swept in BF16 or FP16 storage
  * with FP32 accumulation, and u += e.  In exact arithmetic the result after
  * p->iterations sweeps is that of p->iterations plain sweeps.  With tol > 0
- * the solve stops once the FP64 relative residual (computed on the GPU every
- * check_every outer steps) drops below tol.  Needs p->mode == JACOBI and
+ * the solve stops once the relative residual (stencil_residual, computed on
+ * the GPU every check_every outer steps) drops below tol.  Needs p->mode == JACOBI and
  * nx % 8 == 0; d_u's border band is never written.  Allocates nothing: the
  * caller passes a 256-byte aligned workspace of stencil_ir_workspace_bytes. */
 enum { STENCIL_STORAGE_FP32 = 0, STENCIL_STORAGE_BF16 = 1, STENCIL_STORAGE_FP16 = 2 };
@@ -208,7 +208,7 @@ typedef struct stencil_ir_params {
 typedef struct stencil_ir_result {
     int sweeps;          /* sweeps performed */
     int outer_steps;     /* refinement steps performed */
-    double rel_residual; /* FP64 relative residual of the final u */
+    double rel_residual; /* relative residual of the final u (stencil_residual) */
 } stencil_ir_result;
 
 STENCIL_API int stencil_ir_workspace_bytes(const stencil_params *p, const stencil_ir_params *ir,
@@ -220,8 +220,12 @@ STENCIL_API int stencil_ir_solve(const stencil_params *p, const stencil_ir_param
 
 /* Relative residual ||b - A u||_2 / ||b||_2 of the steady state that JACOBI
  * iterates to, (A u)(x) = u(x) - mean of the 2*D*R axis neighbours over the
- * update region, b = the border contributions; squares summed in FP64 on the
- * GPU.  Synchronises `stream`. */
+ * update region, b = the border contributions.  Each cell's residual is
+ * evaluated in FP32 as the sum of its (neighbour - centre) differences
+ * (exact wherever neighbour and centre are within a factor of two, so it
+ * stays accurate relative to itself as it shrinks); FP64 is used for the
+ * sums of squares only.  Agrees with an all-FP64 evaluation to about 1e-7
+ * relative.  Synchronises `stream`. */
 STENCIL_API int stencil_residual(const stencil_params *p, const float *d_u, double *rel_residual,
                      stencil_stream_t stream);
 

@@ -44,8 +44,9 @@ def test_ir_matches_fp32_and_fp64(cuda, storage, bound, shape, radius, sweeps):
     band = np.ones(shape, bool)
     band[(slice(radius, -radius),) * len(shape)] = False
     assert np.array_equal(got[band], host[band])
-    # residual as reported equals the oracle's residual of the returned grid
-    assert rel == pytest.approx(O.rel_residual(got, radius), rel=1e-9)
+    # residual as reported equals the oracle's (all-FP64) residual of the
+    # returned grid, up to the FP32 per-cell evaluation
+    assert rel == pytest.approx(O.rel_residual(got, radius), rel=1e-6)
 
 
 def test_ir_converges_to_tolerance(cuda):

@@ -121,7 +121,8 @@ def test_residual_matches_oracle(cuda, shape, radius):
     u = S.init_uniform(shape, 21)
     got = S.residual(u, radius)
     want = O.rel_residual(u.cpu().numpy(), radius)
-    assert got == pytest.approx(want, rel=1e-12)
+    # per-cell residual in FP32 (neighbour - centre differences), squares in FP64
+    assert got == pytest.approx(want, rel=1e-6)
 
 
 def test_run_host_matches_dispatch(cuda):

@@ -11,7 +11,7 @@
 //   3. u += s * e_m in FP32.
 // In exact arithmetic u + s*e_m is exactly m Jacobi sweeps from u, so the
 // total sweep count means the same as for the FP32 loop; only rounding
-// differs.  The FP64 relative residual (k_util.cu) decides convergence when a
+// differs.  The relative residual (k_util.cu; FP64 sums) decides convergence when a
 // tolerance is given.  Correction sweeps move 6 bytes per cell update (read e
 // and r, write e) instead of 8; on 3-D grids they run on the TMA-fed stream
 // form (k_lpstream.cu), elsewhere on k_lp_sweep below (the same arithmetic).
@@ -138,13 +138,30 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// r = (M u + c) - u over the update region (FP32).  pass 0: max |r| into
-// *max_bits.  pass 1: stores r * 2^-ceil(log2 max) in E and the scale in *scale.
+// Rows of the update region are handed to warps round-robin (no 64-bit
+// index division); a lane owns 4-cell chunks of its row (nx % 8 == 0).
+struct IrRows {
+    int R, ry, nrows, nch;
+    __device__ IrRows(const Geom &g, int D, int r) : R(r), ry(g.ny - 2 * r) {
+        nrows = ry * (D == 3 ? g.nz - 2 * r : 1);
+        nch = g.nx >> 2;
+    }
+    __device__ long long base(const Geom &g, int q) const {
+        return (long long)(R + q % ry) * g.sy + (long long)(q / ry + (g.nz > 1 ? R : 0)) * g.sz;
+    }
+};
+
+__device__ __forceinline__ float4 ir_ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+
+// r = (M u + c) - u over the update region (FP32, the sweep's summation
+// order).  pass 0: max |r| into *max_bits.  pass 1: stores r * 2^-ceil(log2
+// max) in E and the scale in *scale.
 template <typename E, int D, int R>
 __global__ void __launch_bounds__(256)
     k_ir_resid(const float *__restrict__ u, E *__restrict__ r, Geom g, unsigned *max_bits,
                float *scale, int pass) {
     constexpr int C = 2 * D * R;
+    constexpr int RA = (R + 3) & ~3;
     float inv = 1.0f;
     if (pass == 1) {
         const float m = __uint_as_float(*max_bits);
@@ -154,30 +171,63 @@ __global__ void __launch_bounds__(256)
         inv = 1.0f / s;
         if (blockIdx.x == 0 && threadIdx.x == 0) *scale = s;
     }
+    const IrRows rows(g, D, R);
+    const int wpb = blockDim.x >> 5, lane = threadIdx.x & 31;
     float local = 0.0f;
-    const long long n = (long long)(g.nx - 2 * R) * (g.ny - 2 * R) * (D == 3 ? g.nz - 2 * R : 1);
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-         c += (long long)gridDim.x * blockDim.x) {
-        const int i = R + (int)(c % (g.nx - 2 * R));
-        const long long q = c / (g.nx - 2 * R);
-        const int j = R + (int)(q % (g.ny - 2 * R));
-        const int k = D == 3 ? R + (int)(q / (g.ny - 2 * R)) : 0;
-        const long long idx = i + (long long)j * g.sy + (long long)k * g.sz;
-        float acc = 0.0f;
+    for (int q = blockIdx.x * wpb + (threadIdx.x >> 5); q < rows.nrows; q += gridDim.x * wpb) {
+        const long long base = rows.base(g, q);
+        const float *row = u + base;
+        for (int c = lane; c < rows.nch; c += 32) {
+            const int x0 = 4 * c;
+            if (x0 + 3 < R || x0 >= g.nx - R) continue;
+            float w[4 + 2 * RA];
 #pragma unroll
-        for (int o = -R; o <= R; ++o)
-            if (o) acc += u[idx + o];
+            for (int h = 0; h < (4 + 2 * RA) / 4; ++h) {
+                const int cc = c - RA / 4 + h;
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (cc >= 0 && cc < rows.nch) v = ir_ld4(row + 4 * cc);
+                w[4 * h] = v.x; w[4 * h + 1] = v.y; w[4 * h + 2] = v.z; w[4 * h + 3] = v.w;
+            }
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int o = -R; o <= R; ++o)
-            if (o) acc += u[idx + o * g.sy];
-        if (D == 3) {
+            for (int o = -R; o <= R; ++o) {
+                if (!o) continue;
 #pragma unroll
-            for (int o = -R; o <= R; ++o)
-                if (o) acc += u[idx + o * g.sz];
+                for (int e = 0; e < 4; ++e) acc[e] += w[RA + e + o];
+            }
+#pragma unroll
+            for (int o = -R; o <= R; ++o) {
+                if (!o) continue;
+                const float4 v = ir_ld4(row + x0 + o * g.sy);
+                acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
+            }
+            if (D == 3) {
+#pragma unroll
+                for (int o = -R; o <= R; ++o) {
+                    if (!o) continue;
+                    const float4 v = ir_ld4(row + x0 + o * g.sz);
+                    acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
+                }
+            }
+            float res[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) res[e] = div_coeff<C>(acc[e]) - w[RA + e];
+            const bool full = x0 >= R && x0 + 3 < g.nx - R;
+            if (pass == 0) {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (full || in_range(x0 + e, g.nx, R)) local = fmaxf(local, fabsf(res[e]));
+            } else if (full) {
+                uint2 q2;
+                q2.x = LowP<E>::from2(res[0] * inv, res[1] * inv);
+                q2.y = LowP<E>::from2(res[2] * inv, res[3] * inv);
+                *reinterpret_cast<uint2 *>(r + base + x0) = q2;
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (in_range(x0 + e, g.nx, R)) r[base + x0 + e] = LowP<E>::from(res[e] * inv);
+            }
         }
-        const float res = div_coeff<C>(acc) - u[idx];
-        if (pass == 0) local = fmaxf(local, fabsf(res));
-        else r[idx] = LowP<E>::from(res * inv);
     }
     if (pass == 0) {
 #pragma unroll
@@ -191,15 +241,27 @@ template <typename E, int D, int R>
 __global__ void __launch_bounds__(256)
     k_ir_update(float *__restrict__ u, const E *__restrict__ e, Geom g, const float *scale) {
     const float s = *scale;
-    const long long n = (long long)(g.nx - 2 * R) * (g.ny - 2 * R) * (D == 3 ? g.nz - 2 * R : 1);
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-         c += (long long)gridDim.x * blockDim.x) {
-        const int i = R + (int)(c % (g.nx - 2 * R));
-        const long long q = c / (g.nx - 2 * R);
-        const int j = R + (int)(q % (g.ny - 2 * R));
-        const int k = D == 3 ? R + (int)(q / (g.ny - 2 * R)) : 0;
-        const long long idx = i + (long long)j * g.sy + (long long)k * g.sz;
-        u[idx] = fmaf(s, LowP<E>::to(e[idx]), u[idx]);
+    const IrRows rows(g, D, R);
+    const int wpb = blockDim.x >> 5, lane = threadIdx.x & 31;
+    for (int q = blockIdx.x * wpb + (threadIdx.x >> 5); q < rows.nrows; q += gridDim.x * wpb) {
+        const long long base = rows.base(g, q);
+        for (int c = lane; c < rows.nch; c += 32) {
+            const int x0 = 4 * c;
+            if (x0 + 3 < R || x0 >= g.nx - R) continue;
+            float *up = u + base + x0;
+            const float4 v = ir_ld4(up);
+            const uint2 ew = *reinterpret_cast<const uint2 *>(e + base + x0);
+            const float2 e01 = LowP<E>::to2(ew.x), e23 = LowP<E>::to2(ew.y);
+            const float out[4] = {fmaf(s, e01.x, v.x), fmaf(s, e01.y, v.y), fmaf(s, e23.x, v.z),
+                                  fmaf(s, e23.y, v.w)};
+            if (x0 >= R && x0 + 3 < g.nx - R) {
+                *reinterpret_cast<float4 *>(up) = make_float4(out[0], out[1], out[2], out[3]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (in_range(x0 + k, g.nx, R)) up[k] = out[k];
+            }
+        }
     }
 }
 

@@ -158,6 +158,8 @@ __global__ void __launch_bounds__(LpShape<R>::THREADS, 1)
     using S = LpShape<R>;
     constexpr int C = 6 * R;
     constexpr int QN = 2 * R + 1;
+    constexpr int PF = R == 4 ? 3 : QN;  // rhs prefetch distance (registers at R = 4)
+    static_assert(QN % PF == 0, "the rhs ring must divide the plane queue");
     constexpr bool PK = R >= 3;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char *ring = reinterpret_cast<unsigned char *>(
@@ -223,18 +225,25 @@ __global__ void __launch_bounds__(LpShape<R>::THREADS, 1)
             qz[p] = to4<E>(*reinterpret_cast<const uint2 *>(ring + s * S::SLOT_BYTES + own));
             if (p < R || p >= np - R) release(s);
         }
-        // rhs of the first plane; later planes are fetched one step ahead
-        uint2 rn = make_uint2(0, 0);
-        if (live) rn = __ldg(reinterpret_cast<const uint2 *>(rhs + (long long)z0 * g.sz + rowoff));
+        // rhs of planes z .. z+PF-1 in a register ring, each fetched PF plane
+        // steps before its use (one step is shorter than a DRAM round trip);
+        // PF divides QN so the ring position is known at compile time
+        uint2 rq[PF];
+#pragma unroll
+        for (int p = 0; p < PF; ++p) {
+            rq[p] = make_uint2(0, 0);
+            if (live && z0 + p < z1)
+                rq[p] = __ldg(reinterpret_cast<const uint2 *>(rhs + (long long)(z0 + p) * g.sz + rowoff));
+        }
         for (int zb = z0; zb < z1; zb += QN) {
 #pragma unroll
             for (int ph = 0; ph < QN; ++ph) {
                 const int z = zb + ph;
                 if (z >= z1) break;
                 const int step = z - z0;
-                const uint2 rc = rn;
-                if (live && z + 1 < z1)
-                    rn = __ldg(reinterpret_cast<const uint2 *>(rhs + (long long)(z + 1) * g.sz + rowoff));
+                const uint2 rc = rq[ph % PF];
+                if (live && z + PF < z1)
+                    rq[ph % PF] = __ldg(reinterpret_cast<const uint2 *>(rhs + (long long)(z + PF) * g.sz + rowoff));
                 const int sc = (qb + step + R) & (kNS - 1);
                 const unsigned char *cb = ring + sc * S::SLOT_BYTES + own;
                 // cells x-4 .. x+7 of row y as six 2-cell words; x- and y-neighbours

@@ -1,5 +1,5 @@
 // k_util.cu -- whole-grid helper kernels: seeded initial states, border copy,
-// and the FP64 residual norm.
+// and the residual norm (FP64 sums).
 #include <algorithm>
 
 #include "host.hpp"
@@ -52,10 +52,15 @@ __global__ void k_copy_border(const float *__restrict__ src, float *__restrict__
     }
 }
 
-// Residual of the JACOBI steady state, accumulated in FP64: per update-region
-// cell r = (sum of neighbours)/(2DR) - u, b = (sum of border neighbours)/(2DR).
-// Stage 1 writes one (sum r^2, sum b^2) pair per block; stage 2 adds the pairs
-// in a fixed order, so the result does not depend on scheduling.
+// Residual of the JACOBI steady state.  Per update-region cell, in FP32:
+// d = sum over the 2DR axis neighbours of (neighbour - centre) (= 2DR r, with
+// r = (sum of neighbours)/(2DR) - u; the differences are exact wherever
+// neighbour and centre are within a factor of two, so r keeps its relative
+// accuracy as it shrinks, unlike sum/(2DR) - u), and bsum = sum of the border
+// neighbours.  FP64 only for the reduction: stage 1 writes one (sum d^2,
+// sum bsum^2) pair per block, stage 2 adds the pairs in a fixed order (the
+// result does not depend on scheduling) and divides by (2DR)^2.  One warp per
+// row of the update region (rows handed out round-robin), lanes along x.
 constexpr int kResidBlocks = 1024;
 constexpr int kResidThreads = 256;
 
@@ -84,47 +89,50 @@ __global__ void __launch_bounds__(kResidThreads)
     k_residual_partial(const float *__restrict__ u, Geom g, int dims, double *__restrict__ part) {
     __shared__ double sh[2 * (kResidThreads / 32)];
     const int R = g.radius;
-    const int ix = g.nx - 2 * R, iy = g.ny - 2 * R, iz = dims == 3 ? g.nz - 2 * R : 1;
-    const long long n = (long long)ix * iy * iz;
-    const double coeff = 2.0 * dims * R;
+    const int ry = g.ny - 2 * R, nrows = ry * (dims == 3 ? g.nz - 2 * R : 1);
+    const int wpb = blockDim.x >> 5, lane = threadIdx.x & 31;
     double rr = 0.0, bb = 0.0;
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-         c += (long long)gridDim.x * blockDim.x) {
-        const int i = R + (int)(c % ix);
-        const int j = R + (int)((c / ix) % iy);
-        const int k = dims == 3 ? R + (int)(c / ((long long)ix * iy)) : 0;
-        const long long idx = i + (long long)j * g.sy + (long long)k * g.sz;
-        double all = 0.0, bnd = 0.0;
-        for (int o = -R; o <= R; ++o) {
-            if (!o) continue;
-            const double v = u[idx + o];
-            all += v;
-            if (!in_range(i + o, g.nx, R)) bnd += v;
-        }
-        for (int o = -R; o <= R; ++o) {
-            if (!o) continue;
-            const double v = u[idx + o * g.sy];
-            all += v;
-            if (!in_range(j + o, g.ny, R)) bnd += v;
-        }
-        if (dims == 3)
+    for (int q = blockIdx.x * wpb + (threadIdx.x >> 5); q < nrows; q += gridDim.x * wpb) {
+        const int j = R + q % ry, k = dims == 3 ? R + q / ry : 0;
+        const long long base = (long long)j * g.sy + (long long)k * g.sz;
+        // rows whose y or z neighbours reach the border band
+        const bool near_yz = j < 2 * R || j >= g.ny - 2 * R ||
+                             (dims == 3 && (k < 2 * R || k >= g.nz - 2 * R));
+        for (int i = R + lane; i < g.nx - R; i += 32) {
+            const long long idx = base + i;
+            const float c = u[idx];
+            float d = 0.0f, bs = 0.0f;
             for (int o = -R; o <= R; ++o) {
                 if (!o) continue;
-                const double v = u[idx + o * g.sz];
-                all += v;
-                if (!in_range(k + o, g.nz, R)) bnd += v;
+                const float v = u[idx + o];
+                d += v - c;
+                if (!in_range(i + o, g.nx, R)) bs += v;
             }
-        const double r = all / coeff - (double)u[idx];
-        bnd /= coeff;
-        rr += r * r;
-        bb += bnd * bnd;
+            for (int o = -R; o <= R; ++o) {
+                if (!o) continue;
+                const float v = u[idx + o * g.sy];
+                d += v - c;
+                if (near_yz && !in_range(j + o, g.ny, R)) bs += v;
+            }
+            if (dims == 3)
+                for (int o = -R; o <= R; ++o) {
+                    if (!o) continue;
+                    const float v = u[idx + o * g.sz];
+                    d += v - c;
+                    if (near_yz && !in_range(k + o, g.nz, R)) bs += v;
+                }
+            rr = fma((double)d, (double)d, rr);
+            if (bs != 0.0f) bb = fma((double)bs, (double)bs, bb);
+        }
     }
     block_sum2(rr, bb, sh);
     if (threadIdx.x == 0) { part[2 * blockIdx.x] = rr; part[2 * blockIdx.x + 1] = bb; }
 }
 
+// inv_c2 = 1 / (2DR)^2 turns the sums of d^2 and bsum^2 into sums of r^2 and b^2.
 __global__ void __launch_bounds__(kResidThreads)
-    k_residual_final(const double *__restrict__ part, int nparts, double *__restrict__ out) {
+    k_residual_final(const double *__restrict__ part, int nparts, double *__restrict__ out,
+                     double inv_c2) {
     __shared__ double sh[2 * (kResidThreads / 32)];
     double rr = 0.0, bb = 0.0;
     for (int p = threadIdx.x; p < nparts; p += blockDim.x) {
@@ -132,7 +140,7 @@ __global__ void __launch_bounds__(kResidThreads)
         bb += part[2 * p + 1];
     }
     block_sum2(rr, bb, sh);
-    if (threadIdx.x == 0) { out[0] = rr; out[1] = bb; }
+    if (threadIdx.x == 0) { out[0] = rr * inv_c2; out[1] = bb * inv_c2; }
 }
 
 int launch_init_reference(const Geom &g, int dims, float *u, cudaStream_t s) {
@@ -158,8 +166,9 @@ size_t residual_scratch_bytes() { return (2 * kResidBlocks + 2) * sizeof(double)
 int launch_residual(const Geom &g, int dims, const float *u, double *scratch, cudaStream_t s) {
     k_residual_partial<<<kResidBlocks, kResidThreads, 0, s>>>(u, g, dims, scratch);
     ST_CUDA(cudaGetLastError());
+    const double c = 2.0 * dims * g.radius;
     k_residual_final<<<1, kResidThreads, 0, s>>>(scratch, kResidBlocks,
-                                                  scratch + 2 * kResidBlocks);
+                                                  scratch + 2 * kResidBlocks, 1.0 / (c * c));
     return cuda_fail(cudaGetLastError(), "residual launch");
 }
 

@@ -33,7 +33,7 @@ namespace st {
 __global__ void k_residual_partial(const float *__restrict__ u, Geom g, int dims,
                                    double *__restrict__ part);
 __global__ void k_residual_final(const double *__restrict__ part, int nparts,
-                                 double *__restrict__ out);
+                                 double *__restrict__ out, double inv_c2);
 
 constexpr int kNoAllocThreads = 256;
 constexpr int kNoAllocMaxParts = 16384;
@@ -88,7 +88,9 @@ extern "C" int stencil_residual_noalloc(const stencil_params *p, const float *d_
     const int nparts = parts > 0 ? (int)parts : 1;
     k_residual_partial<<<nparts, kNoAllocThreads, 0, s>>>(d_u, g, p->dims, scratch);
     ST_CUDA(cudaGetLastError());
-    k_residual_final<<<1, kNoAllocThreads, 0, s>>>(scratch, nparts, scratch + 2 * kNoAllocMaxParts);
+    const double c = 2.0 * p->dims * p->radius;
+    k_residual_final<<<1, kNoAllocThreads, 0, s>>>(scratch, nparts, scratch + 2 * kNoAllocMaxParts,
+                                                    1.0 / (c * c));
     ST_CUDA(cudaGetLastError());
     double sums[2];
     ST_CUDA(cudaMemcpyAsync(sums, scratch + 2 * kNoAllocMaxParts, sizeof sums,
