@@ -13,9 +13,9 @@
 //     rounding, no separate conversion); its rhs values come from global
 //     memory one plane ahead;
 //   * the sum runs in the order of the FP32 sweep (axis i, j, k; offsets -R..-1,
-//     +1..+R), starts from its first term, and is divided as there, then rhs
-//     is added, so each cell equals the cell-by-cell correction sweep
-//     (k_lp_sweep, k_ir.cu) bit for bit.
+//     +1..+R) and starts from its first term; sum / C + rhs is one fused
+//     multiply-add by RN(1/C) (within an FP32 ulp of the division, far below
+//     the 16-bit storage rounding).
 // Per cell update it reads 4 bytes (e and rhs) and writes 2, against 8 for an
 // FP32 sweep; the border band of e_out is never written.
 #include <cuda_bf16.h>
@@ -131,11 +131,6 @@ __device__ __forceinline__ void add_q(float4 v, float (&acc)[4]) {
     }
 }
 
-template <bool PK, int C>
-__device__ __forceinline__ float2 div_pair(float2 a) {
-    if constexpr (PK) return div_fast2<C>(a);
-    else return make_float2(div_fast<C>(a.x), div_fast<C>(a.y));
-}
 
 constexpr int kTX = 128, kTY = 16, kNS = 16, kRA = 8;
 
@@ -148,10 +143,12 @@ struct LpShape {
     static constexpr int CWARPS = kTY;  // one warp per row, 4 cells per lane
     static constexpr int THREADS = 32 * CWARPS + 32;
     static constexpr int SMEM_BYTES = kNS * SLOT_BYTES + 128 + 2 * kNS * 8;
+    // two CTAs per SM where the registers allow it (R = 1: 34 warps per SM)
+    static constexpr int MIN_BLOCKS = R == 1 ? 2 : 1;
 };
 
 template <typename E, int R>
-__global__ void __launch_bounds__(LpShape<R>::THREADS, 1)
+__global__ void __launch_bounds__(LpShape<R>::THREADS, LpShape<R>::MIN_BLOCKS)
     k_lp_stream(const __grid_constant__ CUtensorMap e_map, E *__restrict__ eo,
                 const E *__restrict__ rhs, Geom g, int tiles_x, int tiles_y, int zchunk,
                 int items) {
@@ -280,19 +277,22 @@ __global__ void __launch_bounds__(LpShape<R>::THREADS, 1)
 #pragma unroll
                 for (int o = 1; o <= R; ++o) add_q<PK>(qz[(ph + R + o) % QN], acc);
                 if (live) {
+                    // sum / C + rhs as one fused multiply-add by RN(1/C): the
+                    // correction is stored in 16 bits, so the division's last
+                    // FP32 bit is immaterial
                     float out[4];
-                    const bool fast = div_fast_ok<C>(acc[0]) && div_fast_ok<C>(acc[1]) &&
-                                      div_fast_ok<C>(acc[2]) && div_fast_ok<C>(acc[3]);
-                    if (fast) {
-                        const float2 d0 = div_pair<PK, C>(make_float2(acc[0], acc[1]));
-                        const float2 d1 = div_pair<PK, C>(make_float2(acc[2], acc[3]));
-                        out[0] = d0.x; out[1] = d0.y; out[2] = d1.x; out[3] = d1.y;
+                    constexpr float kInv = 1.0f / (float)C;
+                    const float2 r01 = Cvt<E>::two(rc.x), r23 = Cvt<E>::two(rc.y);
+                    if constexpr (PK) {
+                        const float2 a = ffma2(make_float2(acc[0], acc[1]), make_float2(kInv, kInv), r01);
+                        const float2 b = ffma2(make_float2(acc[2], acc[3]), make_float2(kInv, kInv), r23);
+                        out[0] = a.x; out[1] = a.y; out[2] = b.x; out[3] = b.y;
                     } else {
-#pragma unroll
-                        for (int e = 0; e < 4; ++e)
-                            out[e] = div_fast_ok<C>(acc[e]) ? div_fast<C>(acc[e]) : div_slow_from_first<C>(acc[e]);
+                        out[0] = fmaf(acc[0], kInv, r01.x);
+                        out[1] = fmaf(acc[1], kInv, r01.y);
+                        out[2] = fmaf(acc[2], kInv, r23.x);
+                        out[3] = fmaf(acc[3], kInv, r23.y);
                     }
-                    add_row<E>(rc, out);  // + rhs
                     E *dst = eo + (long long)z * g.sz + rowoff;
                     if (xin) {
                         uint2 o2;
@@ -323,6 +323,8 @@ int run_lp(const Geom &g, const E *e, E *eo, const E *rhs, cudaStream_t s) {
     int per_sm = (dev >= 0 && dev < 64) ? per_sm_cached[dev] : 0;
     if (!per_sm) {
         ST_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM_BYTES));
+        ST_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     cudaSharedmemCarveoutMaxShared));
         ST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, S::THREADS, S::SMEM_BYTES));
         if (per_sm < 1) return fail(STENCIL_EUNSUPPORTED, "low-precision stream kernel does not fit");
         if (dev >= 0 && dev < 64) per_sm_cached[dev] = per_sm;

@@ -85,13 +85,29 @@ __device__ __forceinline__ void block_sum2(double &a, double &b, double *sh) {
     }
 }
 
+// Adds d^2 to the unevaluated FP32 pair (s + cs): the exact error of the
+// square (fma) and of the addition (TwoSum, Knuth) go into cs, so the pair
+// carries the sum to about FP32^2 precision without FP64 arithmetic per cell
+// (GB300's FP64 rate would bind the kernel).  Explicit roundings: nothing is
+// contracted into fused operations.
+__device__ __forceinline__ void acc_square(float d, float &s, float &cs) {
+    const float p = __fmul_rn(d, d);
+    const float pe = fmaf(d, d, -p);
+    const float t = __fadd_rn(s, p);
+    const float z = __fsub_rn(t, s);
+    cs = __fadd_rn(cs, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z)), pe));
+    s = t;
+}
+
+// Any radius and nx: one lane per cell of a row.
 __global__ void __launch_bounds__(kResidThreads)
-    k_residual_partial(const float *__restrict__ u, Geom g, int dims, double *__restrict__ part) {
+    k_residual_partial_any(const float *__restrict__ u, Geom g, int dims, double *__restrict__ part) {
     __shared__ double sh[2 * (kResidThreads / 32)];
     const int R = g.radius;
     const int ry = g.ny - 2 * R, nrows = ry * (dims == 3 ? g.nz - 2 * R : 1);
     const int wpb = blockDim.x >> 5, lane = threadIdx.x & 31;
-    double rr = 0.0, bb = 0.0;
+    double bb = 0.0;
+    float s = 0.0f, cs = 0.0f;
     for (int q = blockIdx.x * wpb + (threadIdx.x >> 5); q < nrows; q += gridDim.x * wpb) {
         const int j = R + q % ry, k = dims == 3 ? R + q / ry : 0;
         const long long base = (long long)j * g.sy + (long long)k * g.sz;
@@ -121,10 +137,90 @@ __global__ void __launch_bounds__(kResidThreads)
                     d += v - c;
                     if (near_yz && !in_range(k + o, g.nz, R)) bs += v;
                 }
-            rr = fma((double)d, (double)d, rr);
+            acc_square(d, s, cs);
             if (bs != 0.0f) bb = fma((double)bs, (double)bs, bb);
         }
     }
+    double rr = (double)s + (double)cs;
+    block_sum2(rr, bb, sh);
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = rr; part[2 * blockIdx.x + 1] = bb; }
+}
+
+// nx % 4 == 0 and R <= 4: a lane owns 4-cell chunks of its row and issues
+// every neighbour load of a chunk (3 + 2R or 3 + 4R float4) before using any.
+template <int D, int R>
+__global__ void __launch_bounds__(kResidThreads)
+    k_residual_partial_vec(const float *__restrict__ u, Geom g, double *__restrict__ part) {
+    __shared__ double sh[2 * (kResidThreads / 32)];
+    const int ry = g.ny - 2 * R, nrows = ry * (D == 3 ? g.nz - 2 * R : 1);
+    const int nch = g.nx >> 2;
+    const int wpb = blockDim.x >> 5, lane = threadIdx.x & 31;
+    double bb = 0.0;
+    float s = 0.0f, cs = 0.0f;
+    for (int q = blockIdx.x * wpb + (threadIdx.x >> 5); q < nrows; q += gridDim.x * wpb) {
+        const int j = R + q % ry, k = D == 3 ? R + q / ry : 0;
+        const float *row = u + (long long)j * g.sy + (long long)k * g.sz;
+        const bool near_yz = j < 2 * R || j >= g.ny - 2 * R ||
+                             (D == 3 && (k < 2 * R || k >= g.nz - 2 * R));
+        for (int cc = lane; cc < nch; cc += 32) {
+            const int x0 = 4 * cc;
+            if (x0 + 3 < R || x0 >= g.nx - R) continue;
+            const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 l4 = cc > 0 ? *reinterpret_cast<const float4 *>(row + x0 - 4) : z4;
+            const float4 m4 = *reinterpret_cast<const float4 *>(row + x0);
+            const float4 r4 = cc + 1 < nch ? *reinterpret_cast<const float4 *>(row + x0 + 4) : z4;
+            float4 yz[(D == 3 ? 4 : 2) * R];
+#pragma unroll
+            for (int o = 1; o <= R; ++o) {
+                yz[2 * (o - 1)] = *reinterpret_cast<const float4 *>(row + x0 - o * g.sy);
+                yz[2 * (o - 1) + 1] = *reinterpret_cast<const float4 *>(row + x0 + o * g.sy);
+                if (D == 3) {
+                    yz[2 * R + 2 * (o - 1)] = *reinterpret_cast<const float4 *>(row + x0 - o * g.sz);
+                    yz[2 * R + 2 * (o - 1) + 1] = *reinterpret_cast<const float4 *>(row + x0 + o * g.sz);
+                }
+            }
+            const float w[12] = {l4.x, l4.y, l4.z, l4.w, m4.x, m4.y, m4.z, m4.w, r4.x, r4.y, r4.z, r4.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int i = x0 + e;
+                if (!in_range(i, g.nx, R)) continue;
+                const float c = w[4 + e];
+                float d = 0.0f, bs = 0.0f;
+#pragma unroll
+                for (int o = -R; o <= R; ++o) {
+                    if (!o) continue;
+                    const float v = w[4 + e + o];
+                    d += v - c;
+                    if (!in_range(i + o, g.nx, R)) bs += v;
+                }
+#pragma unroll
+                for (int o = 1; o <= R; ++o) {
+                    const float vm = (&yz[2 * (o - 1)].x)[e], vp = (&yz[2 * (o - 1) + 1].x)[e];
+                    d += vm - c;
+                    d += vp - c;
+                    if (near_yz) {
+                        if (!in_range(j - o, g.ny, R)) bs += vm;
+                        if (!in_range(j + o, g.ny, R)) bs += vp;
+                    }
+                }
+                if (D == 3) {
+#pragma unroll
+                    for (int o = 1; o <= R; ++o) {
+                        const float vm = (&yz[2 * R + 2 * (o - 1)].x)[e], vp = (&yz[2 * R + 2 * (o - 1) + 1].x)[e];
+                        d += vm - c;
+                        d += vp - c;
+                        if (near_yz) {
+                            if (!in_range(k - o, g.nz, R)) bs += vm;
+                            if (!in_range(k + o, g.nz, R)) bs += vp;
+                        }
+                    }
+                }
+                acc_square(d, s, cs);
+                if (bs != 0.0f) bb = fma((double)bs, (double)bs, bb);
+            }
+        }
+    }
+    double rr = (double)s + (double)cs;
     block_sum2(rr, bb, sh);
     if (threadIdx.x == 0) { part[2 * blockIdx.x] = rr; part[2 * blockIdx.x + 1] = bb; }
 }
@@ -163,13 +259,40 @@ int launch_init_uniform(float *u, size_t count, uint64_t seed, cudaStream_t s) {
 // scratch: >= residual_scratch_bytes() of device memory, 8-byte aligned.
 size_t residual_scratch_bytes() { return (2 * kResidBlocks + 2) * sizeof(double); }
 
-int launch_residual(const Geom &g, int dims, const float *u, double *scratch, cudaStream_t s) {
-    k_residual_partial<<<kResidBlocks, kResidThreads, 0, s>>>(u, g, dims, scratch);
-    ST_CUDA(cudaGetLastError());
-    const double c = 2.0 * dims * g.radius;
-    k_residual_final<<<1, kResidThreads, 0, s>>>(scratch, kResidBlocks,
-                                                  scratch + 2 * kResidBlocks, 1.0 / (c * c));
+// Stage 1 over `blocks` blocks (any count: rows are handed out round-robin).
+int launch_residual_partial(const Geom &g, int dims, const float *u, double *part, int blocks,
+                            cudaStream_t s) {
+    const bool vec = g.nx % 4 == 0 && g.radius <= 4;
+    if (!vec) {
+        k_residual_partial_any<<<blocks, kResidThreads, 0, s>>>(u, g, dims, part);
+    } else {
+        const int key = dims * 10 + g.radius;
+        switch (key) {
+            case 21: k_residual_partial_vec<2, 1><<<blocks, kResidThreads, 0, s>>>(u, g, part); break;
+            case 22: k_residual_partial_vec<2, 2><<<blocks, kResidThreads, 0, s>>>(u, g, part); break;
+            case 23: k_residual_partial_vec<2, 3><<<blocks, kResidThreads, 0, s>>>(u, g, part); break;
+            case 24: k_residual_partial_vec<2, 4><<<blocks, kResidThreads, 0, s>>>(u, g, part); break;
+            case 31: k_residual_partial_vec<3, 1><<<blocks, kResidThreads, 0, s>>>(u, g, part); break;
+            case 32: k_residual_partial_vec<3, 2><<<blocks, kResidThreads, 0, s>>>(u, g, part); break;
+            case 33: k_residual_partial_vec<3, 3><<<blocks, kResidThreads, 0, s>>>(u, g, part); break;
+            default: k_residual_partial_vec<3, 4><<<blocks, kResidThreads, 0, s>>>(u, g, part); break;
+        }
+    }
     return cuda_fail(cudaGetLastError(), "residual launch");
 }
+
+int launch_residual_final(const Geom &g, int dims, const double *part, int nparts, double *out,
+                          cudaStream_t s) {
+    const double c = 2.0 * dims * g.radius;
+    k_residual_final<<<1, kResidThreads, 0, s>>>(part, nparts, out, 1.0 / (c * c));
+    return cuda_fail(cudaGetLastError(), "residual launch");
+}
+
+int launch_residual(const Geom &g, int dims, const float *u, double *scratch, cudaStream_t s) {
+    int rc = launch_residual_partial(g, dims, u, scratch, kResidBlocks, s);
+    if (rc) return rc;
+    return launch_residual_final(g, dims, scratch, kResidBlocks, scratch + 2 * kResidBlocks, s);
+}
+
 
 }  // namespace st

@@ -28,14 +28,12 @@
 
 namespace st {
 
-// Kernels of the regular residual path (k_util.cu), compiled with
-// __launch_bounds__(256).
-__global__ void k_residual_partial(const float *__restrict__ u, Geom g, int dims,
-                                   double *__restrict__ part);
-__global__ void k_residual_final(const double *__restrict__ part, int nparts,
-                                 double *__restrict__ out, double inv_c2);
+// The two stages of the regular residual path (k_util.cu; 256-thread blocks).
+int launch_residual_partial(const Geom &g, int dims, const float *u, double *part, int blocks,
+                            cudaStream_t s);
+int launch_residual_final(const Geom &g, int dims, const double *part, int nparts, double *out,
+                          cudaStream_t s);
 
-constexpr int kNoAllocThreads = 256;
 constexpr int kNoAllocMaxParts = 16384;
 constexpr long long kNoAllocCellsPerPart = 65536;
 
@@ -86,12 +84,9 @@ extern "C" int stencil_residual_noalloc(const stencil_params *p, const float *d_
     if (rc) return rc;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const int nparts = parts > 0 ? (int)parts : 1;
-    k_residual_partial<<<nparts, kNoAllocThreads, 0, s>>>(d_u, g, p->dims, scratch);
-    ST_CUDA(cudaGetLastError());
-    const double c = 2.0 * p->dims * p->radius;
-    k_residual_final<<<1, kNoAllocThreads, 0, s>>>(scratch, nparts, scratch + 2 * kNoAllocMaxParts,
-                                                    1.0 / (c * c));
-    ST_CUDA(cudaGetLastError());
+    rc = launch_residual_partial(g, p->dims, d_u, scratch, nparts, s);
+    if (!rc) rc = launch_residual_final(g, p->dims, scratch, nparts, scratch + 2 * kNoAllocMaxParts, s);
+    if (rc) return rc;
     double sums[2];
     ST_CUDA(cudaMemcpyAsync(sums, scratch + 2 * kNoAllocMaxParts, sizeof sums,
                             cudaMemcpyDeviceToHost, s));
