@@ -143,8 +143,8 @@ struct LpShape {
     static constexpr int CWARPS = kTY;  // one warp per row, 4 cells per lane
     static constexpr int THREADS = 32 * CWARPS + 32;
     static constexpr int SMEM_BYTES = kNS * SLOT_BYTES + 128 + 2 * kNS * 8;
-    // two CTAs per SM where the registers allow it (R = 1: 34 warps per SM)
-    static constexpr int MIN_BLOCKS = R == 1 ? 2 : 1;
+    // two CTAs per SM where the registers allow it (R <= 2: 34 warps per SM)
+    static constexpr int MIN_BLOCKS = R <= 2 ? 2 : 1;
 };
 
 template <typename E, int R>

@@ -52,9 +52,9 @@ def main(case):
         a, b = u.clone(), u.clone()
         for _ in range(4):
             S.sweep(a, b, 1, 1000, J, "auto")
-    elif case in ("ir_r1", "ir_r4"):
+    elif case in ("ir_r1", "ir_r2", "ir_r4"):
         # mixed-precision refinement, 512^3, 100 sweeps in outer steps of 50
-        R = 1 if case == "ir_r1" else 4
+        R = int(case[-1])
         u = S.init_fourier((512, 512, 512), 1, R)
         for _ in range(2):
             S.ir_solve(u, R, 100, "bf16", inner_sweeps=50)
