@@ -210,10 +210,13 @@ __global__ void __launch_bounds__(kTb2Threads, 1)
     int cur = 0;  // shared buffer holding the newest state
     unsigned blk = 0;
     for (int done = 0; done < iters;) {
+        int4 rg_next = s_region[0];
         for (int k = 1; k <= kk; ++k) {
             const float *src = cur ? S1 : S0;
             float *dst = cur ? S0 : S1;
-            const int4 rg = s_region[k - 1];
+            // this sweep's region, read before the previous sweep's barrier
+            const int4 rg = rg_next;
+            if (k < kk) rg_next = s_region[k];
 #pragma unroll
             for (int i = 0; i < NI; ++i) {
                 if (icol[i] < rg.x || icol[i] >= rg.y || irow[i] < rg.z || irow[i] >= rg.w) continue;
