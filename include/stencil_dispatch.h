@@ -65,7 +65,8 @@ enum {
     STENCIL_VARIANT_SMEM_PADDED = 3,   /* same kernel as SMEM */
     STENCIL_VARIANT_SMEM_REGISTER = 4, /* 2.5D stream along the slowest axis */
     STENCIL_VARIANT_COOP = 5,          /* all sweeps in one cooperative launch; 3-D: one
-                                          sweep (temporal 1) or several per HBM pass;
+                                          sweep per HBM pass (temporal 0 or 1) or
+                                          `temporal` (>= 2, JACOBI, R <= 2) per pass;
                                           2-D grids of at most one tile per SM: every SM,
                                           `temporal` sweeps per halo exchange, tile
                                           block_x * coarsen_x by block_y cells (0: chosen) */
