@@ -359,6 +359,21 @@ __device__ __forceinline__ void stg4(float *p, float a, float b, float c, float 
                  : "memory");
 }
 
+// L2 policy for data written once and not read again soon (a sweep's
+// output): evict first, so it does not displace the rows other CTAs are
+// about to re-read as halos.
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+__device__ __forceinline__ void stg4_hint(float *p, float a, float b, float c, float d, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(a),
+                 "f"(b), "f"(c), "f"(d), "l"(pol)
+                 : "memory");
+}
+
 __device__ __forceinline__ float f4get(const float4 &v, int c) {
     return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
 }
