@@ -173,8 +173,8 @@ STENCIL_API int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, 
                                       stencil_stream_t stream);
 /* Runs the prepared jobs: one persistent cluster launch over a device work
  * queue (every cluster the device can hold) for the jobs that a cluster
- * sweeps, then, for each 3-D job too large for a cluster's shared memory,
- * one persistent whole-GPU launch.  Resets the queue counter first.
+ * sweeps, then, for each job too large for a cluster's shared memory, one
+ * persistent whole-GPU launch.  Resets the queue counter first.
  * Asynchronous; allocates nothing; can be captured into a CUDA graph (the
  * queue reset is a memset node, so every replay runs the whole batch
  * again). */

@@ -108,3 +108,27 @@ def test_tb2d_graph_replay(cuda):
         g.replay()
         torch.cuda.synchronize()
         assert bits_equal(res.cpu().numpy(), want)
+
+
+ROWS_CASES = [((1024, 1024), 1, 9), ((1030, 996), 2, 7), ((768, 2048), 4, 5), ((1024, 1024), 3, 1),
+              ((1536, 1536), 1, 2)]
+
+
+@pytest.mark.parametrize("case", ROWS_CASES, ids=lambda c: "x".join(map(str, c[0])) + "_r%d_i%d" % c[1:])
+@pytest.mark.parametrize("mode", [O.LEGACY, O.JACOBI], ids=["legacy", "jacobi"])
+def test_rows2d_matches_oracle(cuda, case, mode):
+    """2-D grids too large for one tile per SM: every sweep in one cooperative
+    launch with a grid barrier between sweeps (k_rows2d), bit for bit."""
+    shape, radius, iters = case
+    got, got_other, want, other, engine, launches = run_case(shape, radius, iters, mode)
+    assert engine == "rows2d-persistent" and launches == 1
+    assert bits_equal(got, want)
+    assert bits_equal(got_other, other)
+
+
+def test_auto_picks_rows2d_for_large_2d(cuda):
+    import torch
+    from thesis_gb300 import stencil as S
+    u = S.init_uniform((2048, 2048), 3)
+    S.sweep(u, u.clone(), 1, 16, O.JACOBI, "auto")
+    assert S.last_dispatch() == ("rows2d-persistent", 1)

@@ -229,8 +229,10 @@ void note_launches(const char *engine, long long n) {
 
 static int choose_variant(const stencil_params &p) {
     const Geom g = make_geom(p);
-    // small 2-D grids: every SM, temporally blocked (2-5x the one-cluster engine)
-    if (p.dims == 2 && p.iterations >= 8 && tb2d_supported(g, 2)) return STENCIL_VARIANT_COOP;
+    // 2-D: small grids every SM, temporally blocked (2-5x the one-cluster
+    // engine); larger ones every sweep in one persistent launch
+    if (p.dims == 2 && p.iterations >= 8 && (tb2d_supported(g, 2) || rows2d_supported(g, 2)))
+        return STENCIL_VARIANT_COOP;
     if (p.iterations >= 8 && cluster_resident(g, p.dims)) return STENCIL_VARIANT_CLUSTER;
     if (p.dims == 3 && stream3d_supported(g)) return STENCIL_VARIANT_SMEM_REGISTER;
     return STENCIL_VARIANT_BASE;
@@ -317,6 +319,13 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
         float *res = nullptr;
         rc = run_tb2d(g, cur, nxt, p->iterations, p->temporal,
                       p->block_x * std::max(p->coarsen_x, 1), p->block_y, s, &res);
+        if (rc) return rc;
+        if (d_result) *d_result = res;
+        return STENCIL_OK;
+    }
+    if (variant == STENCIL_VARIANT_COOP && p->dims == 2 && rows2d_supported(g, 2)) {
+        float *res = nullptr;
+        rc = run_rows2d(g, cur, nxt, p->iterations, s, &res);
         if (rc) return rc;
         if (d_result) *d_result = res;
         return STENCIL_OK;

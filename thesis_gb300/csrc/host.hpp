@@ -67,6 +67,10 @@ bool tb2d_supported(const Geom &g, int dims);
 int run_tb2d(const Geom &g, float *a, float *b, int iters, int temporal, int tile_x, int tile_y,
              cudaStream_t s, float **res);
 void tb2d_release();
+// Larger 2-D grids: all sweeps in one cooperative launch, a grid-wide barrier
+// between sweeps, register-queue columns (k_rows2d.cu).
+bool rows2d_supported(const Geom &g, int dims);
+int run_rows2d(const Geom &g, float *a, float *b, int iters, cudaStream_t s, float **res);
 // All sweeps of one grid on one thread-block cluster (k_cluster.cu).
 int run_cluster(const Geom &g, int dims, float *a, float *b, int iters, cudaStream_t s,
                 float **res);

@@ -523,14 +523,17 @@ struct BatchHeader {
     int clusters;
 };
 
-// A 3-D job too large for a cluster's shared memory: swept by the whole GPU
-// (the persistent stream kernel, one cooperative launch per job) after the
-// cluster jobs, instead of by one 16-SM cluster from L2/HBM (about twice the
-// throughput on the 128-grid benchmark batch).
+// A job too large for a cluster's shared memory: swept by the whole GPU
+// after the cluster jobs (one cooperative launch per job: the persistent
+// stream kernel for 3-D; for 2-D the temporally blocked engine where the grid
+// fits one tile per SM, else the persistent rows kernel) instead of by one
+// 16-SM cluster from L2/HBM (about twice the throughput on the 128-grid 3-D
+// part of the benchmark batch).
 struct StreamedJob {
     Geom g;
     float *a, *b;
     int iters;
+    int dims;
 };
 
 struct BatchPlan {
@@ -606,8 +609,9 @@ extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, i
             return fail(STENCIL_EUNSUPPORTED, "job %d: batch jobs need nx %% 4 == 0 and radius <= 4", i);
         const Geom g = make_geom(p);
         ClusterJob j = make_job(g, p.dims, b.d_u1, b.d_u2, b.iterations, csize);
-        if (p.dims == 3 && !j.resident && stream3d_supported(g)) {
-            plan.streamed.push_back({g, b.d_u1, b.d_u2, b.iterations});
+        if (!j.resident && ((p.dims == 3 && stream3d_supported(g)) ||
+                            (p.dims == 2 && rows2d_supported(g, 2)))) {
+            plan.streamed.push_back({g, b.d_u1, b.d_u2, b.iterations, p.dims});
             continue;
         }
         table.push_back(j);
@@ -652,7 +656,9 @@ extern "C" int stencil_batch_launch(const void *d_workspace, stencil_stream_t st
         if (rc) return rc;
     }
     for (const StreamedJob &j : plan.streamed) {
-        int rc = run_stream3d(j.g, j.a, j.b, j.iters, 0, 0, s, nullptr, 0, true);
+        int rc = j.dims == 3 ? run_stream3d(j.g, j.a, j.b, j.iters, 0, 0, s, nullptr, 0, true)
+                 : tb2d_supported(j.g, 2) ? run_tb2d(j.g, j.a, j.b, j.iters, 0, 0, 0, s, nullptr)
+                                          : run_rows2d(j.g, j.a, j.b, j.iters, s, nullptr);
         if (rc) return rc;
     }
     return STENCIL_OK;
