@@ -58,11 +58,13 @@ def variant_space(shape, radius):
         sub["smem_padded"] = {"block": [b for b in block_shapes(dims) if b[0] <= 64]}
         if dims == 3 and radius <= 4:
             top.append({"variant": "smem_register"})
-            # default shape, 64 x 32 tiles, one row per thread, 16-slot ring,
-            # 128 x 32 tiles (R <= 2) or 16 one-row warps (R >= 3), and
+            # default shape (R <= 2: one row per thread with a 16-slot ring;
+            # R >= 3: 16 one-row warps), 64 x 32 tiles, one row per thread
+            # with 8 slots, 128 x 16 tiles with two rows per thread and a
+            # 16-slot ring (R >= 3), 128 x 32 tiles (R <= 2), and
             # (nx % 128 == 0, nx <= 512) the full-width row-slab kernel
-            sub["smem_register"] = {"block": [(0, 0, 0), (16, 32, 1), (0, 1, 0), (0, 0, 3),
-                                              (0, 0, 5 if radius <= 2 else 4),
+            sub["smem_register"] = {"block": [(0, 0, 0), (16, 32, 1), (0, 1, 0),
+                                              (0, 0, 5 if radius <= 2 else 3),
                                               (0, 8, 0), (0, 8, 1)]}
         if radius <= 4:
             top.append({"variant": "cluster"})

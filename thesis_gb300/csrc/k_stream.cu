@@ -366,8 +366,8 @@ StreamKernel sk() {
 // per thread (more warps, fewer registers each); 3 = a 16-slot ring (more
 // planes in flight, one CTA per SM); 4 (R >= 3) = 128 x 16, one row per
 // thread, 16 consumer warps in one CTA; 5 (R <= 2) = 128 x 32, two rows per
-// thread (half the y-halo rows per output row).  The default shape of each
-// radius also has the persistent form.
+// thread (half the y-halo rows per output row).  The persistent form exists
+// for the shape it uses (R = 1: 3, R = 2: 5, R >= 3: 4).
 StreamKernel pick(int r, int shape) {
     switch (r) {
         case 1: return shape == 5 ? sk<1, 128, 32, 2, 8>() : shape == 3 ? sk<1, 128, 16, 1, 16, true>() : shape == 2 ? sk<1, 128, 16, 1, 8>() : shape == 1 ? sk<1, 64, 32, 2, 8>() : sk<1, 128, 16, 2, 8>();
@@ -425,11 +425,16 @@ bool stream3d_supported(const Geom &g) {
 int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int tile_y,
                  cudaStream_t s, float **res, int shape_hint, bool persistent) {
     const int R = g.radius;
-    // Defaults measured fastest at 512^3 on GB300: R = 1 the 16-slot ring
-    // (707 GCell/s vs 615 with 8 slots), R = 2 128 x 32 tiles (709 vs 609 with
-    // 128 x 16), R >= 3 one row per thread in 16 warps (R = 3: 516 vs 423
-    // with two rows per thread; R = 4: 411 vs 403, before the packed sums).
-    int shape = (!tile_x && !tile_y) ? (R == 1 ? 3 : (R == 2 ? 5 : 4))
+    // Defaults measured fastest at 512^3 on GB300 (a launch per sweep,
+    // GCell/s): R <= 2 one row per thread with the 16-slot ring (R = 1: 701
+    // vs 634 with 8 slots and 613 with two rows per thread; R = 2: 692 vs
+    // 674 with 8 slots, 616 with 128 x 32 tiles and 581 with two rows), R >= 3
+    // one row per thread in 16 warps (R = 3: 574 vs 533 with two rows per
+    // thread; R = 4: 542 vs 531 with 8 warps and 491 with two rows).  In the
+    // persistent form R = 2 uses 128 x 32 tiles: 709 GCell/s at 512^3 with
+    // either shape, and neither wins across 96^3 to 384^3 (within 10 %
+    // either way).
+    int shape = (!tile_x && !tile_y) ? (R <= 2 ? 3 : 4)
                                      : (tile_y == 1 ? 2 : ((tile_x && tile_x < 128) || tile_y > 16 ? 1 : 0));
     if (shape_hint >= 1 && shape_hint <= 5) shape = shape_hint;
     if (persistent && !(shape_hint >= 1 && shape_hint <= 5)) shape = R == 1 ? 3 : (R == 2 ? 5 : 4);
