@@ -122,9 +122,13 @@ __global__ void __launch_bounds__(128 * (TY / RY) + 32, 1)
                 const int step = z - z0;
                 const int sc = (qb + step + R) & (NS - 1);
                 const float *cb = ring + sc * slotf + own;
+                // rows -R .. RY-1+R; at R >= 2 the own rows are the centre
+                // plane's entries of the z queue, so only the 2R halo rows
+                // are loaded (as in the stream kernel)
                 float4 col[RY + 2 * R];
 #pragma unroll
-                for (int k = 0; k < RY + 2 * R; ++k) col[k] = rl4(cb + (k - R) * nx);
+                for (int k = 0; k < RY + 2 * R; ++k)
+                    col[k] = (R >= 2 && k >= R && k < R + RY) ? qz[k - R][(ph + R) % QN] : rl4(cb + (k - R) * nx);
                 float acc[RY][4];
 #pragma unroll
                 for (int r = 0; r < RY; ++r) {

@@ -195,9 +195,15 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, Strea
                 // Centre plane z (already waited on as the newest, R steps ago).
                 const int sc = (qb + step + R) & (NS - 1);
                 const float *cb = ring_own + sc * S::SLOT_FLOATS;
-                float4 col[RY + 2 * R];  // the thread's 4 columns, rows -R .. RY-1+R
+                // The thread's 4 columns, rows -R .. RY-1+R.  At R >= 2 its own
+                // rows are taken from the centre plane's entries of the z
+                // queue (the same words of the same slot), so only the 2R halo
+                // rows are loaded (512^3: R = 2 +2 %, R = 3 +5 %, R = 4 +3 %,
+                // 96^3-300^3 R = 2 +7-9 %; R = 1 measured 1-4 % slower).
+                float4 col[RY + 2 * R];
 #pragma unroll
-                for (int k = 0; k < RY + 2 * R; ++k) col[k] = lds4(cb + (k - R) * S::PW);
+                for (int k = 0; k < RY + 2 * R; ++k)
+                    col[k] = (R >= 2 && k >= R && k < R + RY) ? qz[k - R][(ph + R) % QN] : lds4(cb + (k - R) * S::PW);
                 // Sums of cells (0, 1) and (2, 3) of each row as pairs (add_pair),
                 // started from the first term (div_slow_from_first).
                 float2 acc[RY][2];
