@@ -198,6 +198,89 @@ __device__ __forceinline__ void sweep_rows2d(const float *src, float *dst, long 
     }
 }
 
+// 3-D slab sweep with a fixed thread -> column map: thread u owns float4
+// chunk u % chunks of update row R + u / chunks (one 32-bit division per
+// column, none per cell) and marches it through the slab's slices, keeping the
+// column's slices s-R .. s+R in a register queue (one new 16-byte load per
+// slice).  Per 4 cells: 1 + 2 (x-neighbour chunks) + 2R (y rows) loads, where
+// the generic slab sweep re-derives (slice, row, chunk) with 64-bit divisions
+// and issues 3 + 4R loads.  Same per-cell summation order and division.
+template <int R>
+__device__ __forceinline__ void sweep_cols3d(const float *src, float *dst, long long base,
+                                             int s_begin, int s_end, const ClusterJob &j) {
+    constexpr int C = 6 * R;
+    constexpr int RA = (R + 3) & ~3;
+    static_assert(RA == 4, "one neighbour chunk per side");
+    const int nx = j.nx, ny = j.ny, chunks = nx >> 2;
+    const long long sl = (long long)nx * ny;
+    const int rows = ny - 2 * R;
+    const int sb = max(s_begin, R), se = min(s_end, j.nz - R);
+    if (sb >= se || rows <= 0) return;
+    const int cols = rows * chunks;
+    for (int u = threadIdx.x; u < cols; u += blockDim.x) {
+        const int c = u % chunks, row = R + u / chunks;
+        const int x0 = 4 * c;
+        unsigned mask = 0;
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+            if (x0 + e >= R && x0 + e < nx - R) mask |= 1u << e;
+        if (!mask) continue;
+        const long long off = (long long)(sb - base) * sl + (long long)row * nx + x0;
+        const float *col = src + off;  // slice sb of this column
+        float *dcol = dst + off;
+        const bool has_l = c > 0, has_r = c + 1 < chunks;
+        float4 q[2 * R + 1];  // slices s-R .. s+R of this column
+#pragma unroll
+        for (int k = 0; k < 2 * R; ++k) q[k] = ld4(col + (k - R) * sl);
+#pragma unroll 2
+        for (int s = sb; s < se; ++s) {
+            q[2 * R] = ld4(col + R * sl);
+            const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 l4 = has_l ? ld4(col - 4) : z4, r4 = has_r ? ld4(col + 4) : z4;
+            float4 yv[2 * R];
+#pragma unroll
+            for (int o = -R; o <= R; ++o)
+                if (o) yv[o < 0 ? o + R : o + R - 1] = ld4(col + o * nx);
+            const float4 m4 = q[R];
+            const float w[12] = {l4.x, l4.y, l4.z, l4.w, m4.x, m4.y, m4.z, m4.w, r4.x, r4.y, r4.z, r4.w};
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int o = -R; o <= R; ++o) {
+                if (!o) continue;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[e] += w[4 + e + o];
+            }
+#pragma unroll
+            for (int k = 0; k < 2 * R; ++k) {
+                acc[0] += yv[k].x; acc[1] += yv[k].y; acc[2] += yv[k].z; acc[3] += yv[k].w;
+            }
+#pragma unroll
+            for (int o = -R; o <= R; ++o) {
+                if (!o) continue;
+                const float4 v = q[R + o];
+                acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
+            }
+            float out[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                out[e] = div_coeff<C>(acc[e]);
+                if (j.legacy) out[e] -= w[4 + e];
+            }
+            if (mask == 0xFu) {
+                *reinterpret_cast<float4 *>(dcol) = make_float4(out[0], out[1], out[2], out[3]);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if ((mask >> e) & 1) dcol[e] = out[e];
+            }
+#pragma unroll
+            for (int k = 0; k < 2 * R; ++k) q[k] = q[k + 1];
+            col += sl;
+            dcol += sl;
+        }
+    }
+}
+
 // Copies slices [s_begin, s_end) between a global grid and a local slab.
 __device__ __forceinline__ void copy_slices(float *to, const float *from, long long count4) {
     for (long long i = threadIdx.x; i < count4; i += blockDim.x)
@@ -234,7 +317,9 @@ __device__ void run_job(const ClusterJob &j, float *smem, uint32_t rank, uint32_
                 const int ext = (kk - k) * R;
                 const int a = max(s0 - ext, 0), b = min(s1 + ext, S);
                 if (s1 > s0) {
-                    if (D == 2 && (j.nx >> 2) <= (int)blockDim.x)
+                    if constexpr (D == 3)
+                        sweep_cols3d<R>(buf[cur], buf[cur ^ 1], s0 - HT, a, b, j);
+                    else if ((j.nx >> 2) <= (int)blockDim.x)
                         sweep_rows2d<R>(buf[cur], buf[cur ^ 1], s0 - HT, a, b, j);
                     else
                         sweep_slab<D, R>(buf[cur], buf[cur ^ 1], s0 - HT, a, b, j);
@@ -276,7 +361,12 @@ __device__ void run_job(const ClusterJob &j, float *smem, uint32_t rank, uint32_
         const float *src = j.a;
         float *dst = j.b;
         for (int it = 0; it < j.iters; ++it) {
-            sweep_slab<D, R>(src, dst, 0, s0, s1, j);
+            if constexpr (D == 3)
+                sweep_cols3d<R>(src, dst, 0, s0, s1, j);
+            else if ((j.nx >> 2) <= (int)blockDim.x)
+                sweep_rows2d<R>(src, dst, 0, s0, s1, j);
+            else
+                sweep_slab<D, R>(src, dst, 0, s0, s1, j);
             cluster_sync();
             const float *t = src;
             src = dst;
