@@ -95,6 +95,17 @@ def main(case):
         bt = S.Batch(jobs)
         for _ in range(3):
             bt.launch()
+    elif case == "batch_3d_small":
+        # the cluster phase of the benchmark batch's small 3-D part: 18 grids
+        # of 56^3 .. 104^3, R = 2, 100 sweeps each, swept from L2 by clusters
+        jobs = []
+        for k in range(18):
+            n = 56 + 8 * (k % 7)
+            u = S.init_uniform((n, n, n), k)
+            jobs.append((u, u.clone(), 2, 100, J))
+        bt = S.Batch(jobs)
+        for _ in range(3):
+            bt.launch()
     else:
         raise SystemExit("unknown case " + case)
     torch.cuda.synchronize()
