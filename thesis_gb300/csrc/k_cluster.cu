@@ -16,6 +16,10 @@
 //     the grid once per launch;
 //   * global: the slabs are swept from global memory (L2-resident for the
 //     batch sizes) with the same per-cell code.
+// Per-cell code: 3-D slabs by columns of float4 chunks marched along z with
+// a register queue (sweep_cols3d), 2-D slabs by chunk columns of row blocks
+// with a register queue along y (sweep_rows2d, rows of at most 4 * blockDim.x
+// cells), other 2-D rows by the generic sweep (sweep_slab).
 // Cells outside the update region are never written, and both buffers are
 // loaded from the caller's two buffers, so LEGACY (second-buffer border) and
 // JACOBI semantics are exactly those of the ping-pong loop; at the end both
@@ -49,7 +53,8 @@ __device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast
 // One sweep of the cells of slices [s_begin, s_end) (global slice indices).
 // src/dst address slice s at (s - base) * slice_len; the slice stride is
 // slice_len; within a slice the row pitch is nx.  Rows of the update region
-// only; float4 chunks (nx % 4 == 0 required).
+// only; float4 chunks (nx % 4 == 0 required).  Generic form (any D); used for
+// 2-D rows wider than 4 * blockDim.x cells.
 template <int D, int R>
 __device__ __forceinline__ void sweep_slab(const float *src, float *dst, long long base,
                                            int s_begin, int s_end, const ClusterJob &j) {
