@@ -210,7 +210,13 @@ __device__ __forceinline__ void sweep_rows2d(const float *src, float *dst, long 
 // slice).  Per 4 cells: 1 + 2 (x-neighbour chunks) + 2R (y rows) loads, where
 // the generic slab sweep re-derives (slice, row, chunk) with 64-bit divisions
 // and issues 3 + 4R loads.  Same per-cell summation order and division.
-template <int R>
+// PIPE: the loads of slice s+1 are issued before slice s is computed, for the
+// global mode, which is bound by L2 latency (18 grids of 56^3 .. 104^3, R = 2,
+// in one batch: 193.8 GCell/s with the generic sweep, 232.6 with the column
+// sweep, 260.8 with PIPE; R = 1: 220.4 / 259.0 / 325.8); from shared memory
+// the extra registers cost more than the early loads gain (36 grids of
+// 24^3 .. 48^3, R = 2: 102.3 without, 94.5 with).
+template <int R, bool PIPE>
 __device__ __forceinline__ void sweep_cols3d(const float *src, float *dst, long long base,
                                              int s_begin, int s_end, const ClusterJob &j) {
     constexpr int C = 6 * R;
@@ -234,18 +240,45 @@ __device__ __forceinline__ void sweep_cols3d(const float *src, float *dst, long 
         const float *col = src + off;  // slice sb of this column
         float *dcol = dst + off;
         const bool has_l = c > 0, has_r = c + 1 < chunks;
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
         float4 q[2 * R + 1];  // slices s-R .. s+R of this column
 #pragma unroll
         for (int k = 0; k < 2 * R; ++k) q[k] = ld4(col + (k - R) * sl);
-#pragma unroll 2
-        for (int s = sb; s < se; ++s) {
-            q[2 * R] = ld4(col + R * sl);
-            const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 l4 = has_l ? ld4(col - 4) : z4, r4 = has_r ? ld4(col + 4) : z4;
-            float4 yv[2 * R];
+        float4 nq = z4, nl = z4, nr = z4, nyv[2 * R];
+        if constexpr (PIPE) {
+            nq = ld4(col + R * sl);
+            if (has_l) nl = ld4(col - 4);
+            if (has_r) nr = ld4(col + 4);
 #pragma unroll
             for (int o = -R; o <= R; ++o)
-                if (o) yv[o < 0 ? o + R : o + R - 1] = ld4(col + o * nx);
+                if (o) nyv[o < 0 ? o + R : o + R - 1] = ld4(col + o * nx);
+        }
+#pragma unroll 2
+        for (int s = sb; s < se; ++s) {
+            float4 l4, r4, yv[2 * R];
+            if constexpr (PIPE) {
+                q[2 * R] = nq;
+                l4 = nl;
+                r4 = nr;
+#pragma unroll
+                for (int k = 0; k < 2 * R; ++k) yv[k] = nyv[k];
+                if (s + 1 < se) {
+                    const float *nc = col + sl;
+                    nq = ld4(nc + R * sl);
+                    if (has_l) nl = ld4(nc - 4);
+                    if (has_r) nr = ld4(nc + 4);
+#pragma unroll
+                    for (int o = -R; o <= R; ++o)
+                        if (o) nyv[o < 0 ? o + R : o + R - 1] = ld4(nc + o * nx);
+                }
+            } else {
+                q[2 * R] = ld4(col + R * sl);
+                l4 = has_l ? ld4(col - 4) : z4;
+                r4 = has_r ? ld4(col + 4) : z4;
+#pragma unroll
+                for (int o = -R; o <= R; ++o)
+                    if (o) yv[o < 0 ? o + R : o + R - 1] = ld4(col + o * nx);
+            }
             const float4 m4 = q[R];
             const float w[12] = {l4.x, l4.y, l4.z, l4.w, m4.x, m4.y, m4.z, m4.w, r4.x, r4.y, r4.z, r4.w};
             float acc[4] = {0.f, 0.f, 0.f, 0.f};
@@ -323,7 +356,7 @@ __device__ void run_job(const ClusterJob &j, float *smem, uint32_t rank, uint32_
                 const int a = max(s0 - ext, 0), b = min(s1 + ext, S);
                 if (s1 > s0) {
                     if constexpr (D == 3)
-                        sweep_cols3d<R>(buf[cur], buf[cur ^ 1], s0 - HT, a, b, j);
+                        sweep_cols3d<R, false>(buf[cur], buf[cur ^ 1], s0 - HT, a, b, j);
                     else if ((j.nx >> 2) <= (int)blockDim.x)
                         sweep_rows2d<R>(buf[cur], buf[cur ^ 1], s0 - HT, a, b, j);
                     else
@@ -367,7 +400,7 @@ __device__ void run_job(const ClusterJob &j, float *smem, uint32_t rank, uint32_
         float *dst = j.b;
         for (int it = 0; it < j.iters; ++it) {
             if constexpr (D == 3)
-                sweep_cols3d<R>(src, dst, 0, s0, s1, j);
+                sweep_cols3d<R, (R <= 2)>(src, dst, 0, s0, s1, j);  // R >= 3: no register room
             else if ((j.nx >> 2) <= (int)blockDim.x)
                 sweep_rows2d<R>(src, dst, 0, s0, s1, j);
             else
