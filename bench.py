@@ -64,6 +64,24 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world, device):
+    """The largest of every rank's x (a time in seconds): the replicas' step
+    time is the slowest replica's.  Needs the process group when world > 1."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(updates_per_step, steps, world, seconds):
+    """Whole-job GCell-updates/s of `world` replicas that each ran `steps`
+    steps of `updates_per_step` updates in `seconds` (the max over ranks)."""
+    return updates_per_step * steps * world / seconds / 1e9
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -214,11 +232,7 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     def maxed(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return max_over_ranks(x, world, dev)
 
     # ---- headline: device-resident sweeps (radius args.radius) ------------
     barrier()
@@ -230,7 +244,7 @@ def run_ours(args):
     total = maxed(sum(step_times))
     engine, launches_per_step = S.last_dispatch()
     ups = updates(args.dim, args.radius, args.sweeps)
-    value = ups * args.steps * world / total / 1e9
+    value = aggregate_rate(ups, args.steps, world, total)
     # time per sweep (a sweep is one launch, or one grid-barrier phase of the
     # persistent launch; bytes per launch / launch time is the same ratio)
     per_sweep = min(step_times) / args.sweeps
@@ -274,7 +288,7 @@ def run_ours(args):
         ups4 = updates(args.dim, 4, args.sweeps)
         per4 = min(t4) / args.sweeps
         ach4 = ups4 / args.sweeps * HBM_BYTES_PER_UPDATE / per4 / 1e9
-        out["r4"] = {"value": round(ups4 * len(t4) * world / t4s / 1e9, 3),
+        out["r4"] = {"value": round(aggregate_rate(ups4, len(t4), world, t4s), 3),
                      "unit": "GCell-updates/s", "ms_per_step": round(t4s / len(t4) * 1e3, 3),
                      "roofline": {"bound": "hbm", "achieved": round(ach4, 1), "peak": peak,
                                   "unit": "GB/s", "frac": round(ach4 / peak, 4),
@@ -302,7 +316,7 @@ def run_ours(args):
         barrier()
         te = maxed(time.perf_counter() - t0)
         nbytes = h_in.numel() * 4
-        out["e2e"] = {"value": round(ups * args.steps * world / te / 1e9, 3),
+        out["e2e"] = {"value": round(aggregate_rate(ups, args.steps, world, te), 3),
                       "unit": "GCell-updates/s", "h2d_bytes_per_step": nbytes,
                       "d2h_bytes_per_step": nbytes,
                       "api": "stencil_run_host (pinned host in/out, upload + sweeps + download)"}
