@@ -333,7 +333,7 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
     if (variant == STENCIL_VARIANT_COOP && cluster_resident(g, p->dims))
         variant = STENCIL_VARIANT_CLUSTER;
     if (variant == STENCIL_VARIANT_CLUSTER) {
-        if (g.nx % 4 == 0 && g.radius <= 4) {
+        if (cluster_shape_ok(p->dims, g.nx, g.ny, g.radius)) {
             float *res = nullptr;
             rc = run_cluster(g, p->dims, cur, nxt, p->iterations, s, &res);
             if (rc) return rc;

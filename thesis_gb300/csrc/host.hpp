@@ -76,6 +76,9 @@ int run_cluster(const Geom &g, int dims, float *a, float *b, int iters, cudaStre
                 float **res);
 // The grid fits the cluster's shared memory (resident mode).
 bool cluster_resident(const Geom &g, int dims);
+// The cluster engine takes the shape (nx % 4 == 0, R <= 4, 3-D planes of
+// fewer than 2^31 float4 chunks).
+bool cluster_shape_ok(int dims, int nx, int ny, int radius);
 
 // Plain whole-grid helpers.
 int launch_copy_border(const Geom &g, int dims, const float *src, float *dst, cudaStream_t s);

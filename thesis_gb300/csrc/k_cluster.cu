@@ -473,9 +473,16 @@ static long long slab_bytes(const ClusterJob &j, int csize, int tblock) {
     return 2LL * (H + 2 * tblock * j.radius) * slice_len * 4;
 }
 
+// The cluster sweeps read float4 chunks and number a plane's chunk columns
+// with 32-bit integers.
+bool cluster_shape_ok(int dims, int nx, int ny, int radius) {
+    return nx % 4 == 0 && radius >= 1 && radius <= 4 &&
+           (dims == 2 || (long long)(nx / 4) * ny < (1LL << 31));
+}
+
 bool cluster_job_ok(int dims, int nx, int ny, int nz, int radius) {
-    (void)ny; (void)nz; (void)dims;
-    return nx % 4 == 0 && radius >= 1 && radius <= 4;
+    (void)nz;
+    return cluster_shape_ok(dims, nx, ny, radius);
 }
 
 // Resident when the slab fits and every CTA that owns slices owns at least R
@@ -602,8 +609,9 @@ size_t cluster_job_size() { return sizeof(ClusterJob); }
 // Single grid on one cluster, all sweeps in one launch (queue-less mode).
 int run_cluster(const Geom &g, int dims, float *a, float *b, int iters, cudaStream_t s,
                 float **res) {
-    if (g.nx % 4 || g.radius < 1 || g.radius > 4)
-        return fail(STENCIL_EUNSUPPORTED, "cluster engine needs nx %% 4 == 0 and R <= 4");
+    if (!cluster_shape_ok(dims, g.nx, g.ny, g.radius))
+        return fail(STENCIL_EUNSUPPORTED,
+                    "cluster engine needs nx %% 4 == 0, R <= 4 and (3-D) nx/4 * ny < 2^31");
     const int csize = cluster_size_for_device();
     ClusterJob j = make_job(g, dims, a, b, iters, csize);
     int rc = ensure_cluster_attrs();
@@ -631,7 +639,7 @@ int run_cluster(const Geom &g, int dims, float *a, float *b, int iters, cudaStre
 // Whether a single grid is better served by one cluster than by the
 // full-GPU kernels: it fits in the cluster's shared memory.
 bool cluster_resident(const Geom &g, int dims) {
-    if (g.nx % 4 || g.radius < 1 || g.radius > 4) return false;
+    if (!cluster_shape_ok(dims, g.nx, g.ny, g.radius)) return false;
     ClusterJob j = make_job(g, dims, nullptr, nullptr, 0, cluster_size_for_device());
     return j.resident != 0;
 }
