@@ -70,3 +70,27 @@ def test_reference_arm_runs_on_rank_0_only(monkeypatch, capsys):
     monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--gpus", "2"])
     b.run_reference(b.parse())
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_json_contract(monkeypatch, capsys):
+    """bench.py --impl reference on rank 0: one JSON line with the metric of
+    the GPU arm, the CPU baseline it measured and an e2e block without host
+    copies (a small grid here; each step is a bounded sample of about 8 s)."""
+    import json
+    b = _bench()
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--dim", "48",
+                                      "--steps", "1", "--warmup", "0"])
+    b.run_reference(b.parse())
+    line = capsys.readouterr().out.strip().splitlines()[-1]
+    d = json.loads(line)
+    assert d["impl"] == "reference"
+    assert d["unit"] == "GCell-updates/s" and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["steps"] == 1 and d["n_gpus"] == 1
+    assert d["metric"].startswith("GCell-updates/s")
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+    assert d["config"]["dim"] == 48 and d["config"]["radius"] == 1
