@@ -69,8 +69,14 @@ enum {
                                           `temporal` (>= 2, JACOBI, R <= 2) per pass;
                                           2-D grids of at most one tile per SM: every SM,
                                           `temporal` sweeps per halo exchange, tile
-                                          block_x * coarsen_x by block_y cells (0: chosen) */
-    STENCIL_VARIANT_CLUSTER = 6        /* whole grid resident in a thread-block cluster */
+                                          block_x * coarsen_x by block_y cells (0: chosen);
+                                          larger 2-D grids: a grid barrier per sweep
+                                          (nx % 4 == 0, R <= 4); 3-D grids that fit
+                                          one cluster's shared memory go to CLUSTER */
+    STENCIL_VARIANT_CLUSTER = 6        /* all sweeps on one thread-block cluster: the grid
+                                          resident in its shared memory when it fits, else
+                                          swept from L2/HBM (nx % 4 == 0, R <= 4; other
+                                          shapes fall back to COOP) */
 };
 
 /* Runtime description of one sweep loop.  Zero in a tuning field means "choose". */
