@@ -52,8 +52,12 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the 2-D, precision and batching line items")
-    ap.add_argument("--learned", action="store_true",
-                    help="also run the learned-warm-start workload (several minutes)")
+    ap.add_argument("--profile-case", default=None, metavar="NAME",
+                    help="run one small, self-contained case of a hot kernel for a profiler "
+                         "(see PROFILE_CASES) and exit")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned-warm-start workload (about 4 minutes: data, "
+                         "training, 5 x 256 timed solves)")
     return ap.parse_args()
 
 
@@ -158,6 +162,15 @@ class ClockSampler:
             pass
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def bench_config(args, world):
+    """The workload both arms report (the same dict in the reference arm's line)."""
+    return {"workload": "3D %d^3 FP32 star stencil R=%d, Jacobi, %d sweeps per step"
+                        % (args.dim, args.radius, args.sweeps),
+            "dims": 3, "dim": args.dim, "radius": args.radius, "sweeps": args.sweeps,
+            "variant": args.variant, "parallelism": "replicas" if world > 1 else "single",
+            "l2": "no flush: 2 x %d MiB working set > 129 MB L2" % (args.dim ** 3 * 4 // 2 ** 20)}
 
 
 def updates(dim, radius, sweeps):
@@ -265,12 +278,7 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic: border and interior i.i.d. uniform [0,1) (SplitMix64, seed %d)" % SEED,
-        "config": {"workload": "3D %d^3 FP32 star stencil R=%d, Jacobi, %d sweeps per step"
-                               % (args.dim, args.radius, args.sweeps),
-                   "dims": 3, "dim": args.dim, "radius": args.radius, "sweeps": args.sweeps,
-                   "variant": args.variant, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "no flush: 2 x %d MiB working set > 129 MB L2"
-                         % (args.dim ** 3 * 4 // 2 ** 20)},
+        "config": bench_config(args, world),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_kind": peak_kind, "traffic": traffic,
@@ -330,14 +338,21 @@ def run_ours(args):
         out["configs"]["c1_2d_256"] = bench_c1(S, lib, torch)
         out["configs"]["c3_precision_768"] = bench_c3(S, lib, torch)
         out["configs"]["c4_batch_512"] = bench_c4(S, lib, torch)
-        if args.learned:
+        if not args.no_learned:
             from thesis_gb300 import warmstart as W
             seeds = list(range(10_000_000, 10_000_256))
             out["configs"]["c5_learned_512"] = bench_c5(W, torch, seeds)
 
     # ---- CPU baseline: the oracle on the host cores, bounded sample -----------
     if not args.no_cpu and rank == 0:
-        out["cpu_baseline"] = cpu_baseline(u0.cpu().numpy(), args.radius, target_s=10.0)
+        def gpu_sweeps(k):
+            a, b = u0.clone(), u0.clone()
+            res = S.sweep(a, b, args.radius, k, lib.MODE_JACOBI, args.variant)
+            return res.cpu().numpy()
+
+        cb = cpu_baseline(u0.cpu().numpy(), args.radius, target_s=10.0, gpu_sweeps=gpu_sweeps)
+        out["fp64_error"] = cb.pop("check")
+        out["cpu_baseline"] = cb
 
     if rank == 0:
         print(json.dumps(out))
@@ -498,6 +513,11 @@ def bench_c4(S, lib, torch):
 
 
 def bench_c5(W, torch, seeds):
+    """2-D Laplace 512^2 to relative residual 1e-5 on 256 held-out seeds:
+    the learned warm start followed by the FP16 mixed-precision refinement
+    against plain FP32 Jacobi from zero on the same GPU (the library's best
+    plain engine for the grid), every solve timed with CUDA events around
+    all of its GPU work, one problem at a time."""
     from thesis_gb300.unet import UNet
     t0 = time.time()
     fields, sols = W.generate_pairs(20000, 128, sweeps=40000)
@@ -506,14 +526,33 @@ def bench_c5(W, torch, seeds):
     losses, train_s = W.train(net, fields, sols, epochs=40, batch=64, lr=1e-3)
     del fields, sols
     torch.cuda.empty_cache()
-    res = W.evaluate(net, seeds, 512, 1e-5, log=lambda *a: None)
-    res.update({"pairs": 20000, "gen_s": gen_s, "train_s": train_s, "final_loss": losses[-1]})
-    return res
+    arms = ["zero_fp32", "learned_ir_fp16", "learned_fp32", "learned_ir_bf16", "zero_ir_fp16"]
+    res = W.evaluate(net, seeds, 512, 1e-5, arms=arms, n_exact=8, log=lambda *a: None)
+    head, plain = res["learned_ir_fp16"], res["zero_fp32"]
+    return {"workload": "2D Laplace 512^2, 5-point Jacobi to relative residual 1e-5, 256 held-out "
+                        "seeds; U-Net (4 levels, 32 base channels, BF16 weights) trained on 20k "
+                        "128^2 Jacobi-generated pairs",
+            "metric": "time to tolerance per solve, learned warm start + FP16 refinement vs plain "
+                      "FP32 Jacobi from zero",
+            "speedup_vs_plain": round(head["speedup_vs_plain"], 3),
+            "time_to_tol_s": round(head["time_per_solve_s"], 6),
+            "plain_time_to_tol_s": round(plain["time_per_solve_s"], 6),
+            "sweeps": head["mean_sweeps"], "plain_sweeps": plain["mean_sweeps"],
+            "fp64_normwise_err": head["fp64_normwise_err_max"],
+            "plain_fp64_normwise_err": plain["fp64_normwise_err_max"],
+            "arms": {a: res[a] for a in arms},
+            "check_every_plain": res["check_every_plain"], "ir_inner_sweeps": res["ir_inner_sweeps"],
+            "timing": res["timing"], "pairs": 20000, "gen_s": round(gen_s, 1),
+            "train_s": round(train_s, 1), "final_loss": losses[-1]}
 
 
-def cpu_baseline(host_grid, radius, target_s=10.0, threads=None):
+def cpu_baseline(host_grid, radius, target_s=10.0, threads=None, gpu_sweeps=None, check_sweeps=100):
     """Times the oracle's FP32 sweep (CPU restatement of src/stencil_cpu.cu) on
-    the host cores for about target_s seconds of sweeps over the full grid."""
+    the host cores for about target_s seconds of sweeps over the full grid.
+    The same leg checks the GPU against it: gpu_sweeps(k) returns the GPU's
+    grid after k sweeps of the workload, compared with the FP32 oracle (bit
+    for bit: same summation order) and the FP64 oracle (normwise error) after
+    check_sweeps sweeps; returned under "check"."""
     import numpy as np
     from oracle import oracle as O
     threads = threads or os.cpu_count() or 1
@@ -527,22 +566,44 @@ def cpu_baseline(host_grid, radius, target_s=10.0, threads=None):
     t0 = time.perf_counter()
     O.run(a, b, radius, O.JACOBI, n, threads)
     dt = time.perf_counter() - t0
-    return {"value": round(updates(dim, radius, n) / dt / 1e9, 4), "unit": "GCell-updates/s",
-            "cores": threads, "kind": "port",
-            "sample": "%d sweeps of %d^3 R=%d Jacobi (oracle, OpenMP %d threads, %.1f s)"
-                      % (n, dim, radius, threads, dt)}
+    out = {"value": round(updates(dim, radius, n) / dt / 1e9, 4), "unit": "GCell-updates/s",
+           "cores": threads, "kind": "port",
+           "sample": "%d sweeps of %d^3 R=%d Jacobi (oracle, OpenMP %d threads, %.1f s)"
+                     % (n, dim, radius, threads, dt)}
+    del a, b
+    if gpu_sweeps is not None:
+        got = gpu_sweeps(check_sweeps)
+        h = np.ascontiguousarray(host_grid, np.float32)
+        want = O.run(h.copy(), h.copy(), radius, O.JACOBI, check_sweeps, threads)
+        exact = bool(np.array_equal(got.view(np.uint32), want.view(np.uint32)))
+        del want
+        h64 = h.astype(np.float64)
+        r64 = O.run(h64.copy(), h64.copy(), radius, O.JACOBI, check_sweeps, threads)
+        err = float(np.abs(got - r64).max() / np.abs(r64).max())
+        out["check"] = {"sweeps": check_sweeps, "normwise_vs_fp64_oracle": err,
+                        "bit_exact_vs_fp32_oracle": exact,
+                        "what": "GPU grid after %d sweeps of the benchmark workload against the "
+                                "oracle's FP32 and FP64 runs of the same sweeps (the 1000-sweep "
+                                "bit-exact comparison is tests/test_full_iteration_gpu.py)"
+                                % check_sweeps}
+    return out
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU sweep loop (src/stencil_cpu.cu:20-43)
+    timed on the host cores on the same workload.  The reference's own
+    stencil_cpu is built from its sources only where they are present (not on
+    the GPU host), so its bit-identical restatement (the oracle, OpenMP over
+    all host threads) stands in for it.  Each step times a bounded sample of
+    the 1000-sweep workload: `sampled_sweeps_per_step` full-grid sweeps, and
+    `value` is GCell-updates/s over those sweeps."""
     rank, world, local = dist_env()
     if rank != 0:
         return
-    import numpy as np
     from oracle import oracle as O
     shape = (args.dim,) * 3
     u = O.uniform(shape, SEED)
     threads = os.cpu_count() or 1
-    # each step: a bounded sample of the workload (a few sweeps of the full grid)
     a, b = u.copy(), u.copy()
     t0 = time.perf_counter()
     O.sweep(a, b, args.radius, O.JACOBI, threads)
@@ -555,6 +616,10 @@ def run_reference(args):
         O.run(a, b, args.radius, O.JACOBI, per_step, threads)
     dt = time.perf_counter() - t0
     value = updates(args.dim, args.radius, per_step) * args.steps / dt / 1e9
+    sample = ("%d of the %d sweeps per step, full %d^3 grid R=%d (oracle restatement of "
+              "src/stencil_cpu.cu, bit-identical to it, OpenMP %d threads; the reference's "
+              "stencil_cpu is single-threaded and is not built on the GPU host)"
+              % (per_step, args.sweeps, args.dim, args.radius, threads))
     out = {
         "impl": "reference",
         "metric": "GCell-updates/s (3D 512^3 FP32 star stencil, Jacobi, 1000 sweeps)",
@@ -564,27 +629,159 @@ def run_reference(args):
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": round(dt / args.steps * 1e3, 3),
+        "sampled_sweeps_per_step": per_step,
+        "ms_per_step_extrapolated_to_full_step": round(dt / args.steps * args.sweeps / per_step * 1e3, 1),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic: border and interior i.i.d. uniform [0,1) (SplitMix64, seed %d)" % SEED,
-        "config": {"workload": "3D %d^3 FP32 star stencil R=%d, Jacobi, %d sweeps per step"
-                               % (args.dim, args.radius, args.sweeps),
-                   "dims": 3, "dim": args.dim, "radius": args.radius, "sweeps": args.sweeps},
+        "config": bench_config(args, world),
         "cpu_baseline": {"value": round(value, 4), "unit": "GCell-updates/s", "cores": threads,
-                         "kind": "port",
-                         "sample": "%d sweeps per step of %d^3 R=%d (oracle restatement of "
-                                   "src/stencil_cpu.cu, OpenMP %d threads)"
-                                   % (per_step, args.dim, args.radius, threads)},
+                         "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 4), "unit": "GCell-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
 
 
+def _profile_case(case):
+    """Small, self-contained runs of each hot kernel for a profiler: each case
+    warms up, then runs the kernel a few more times.  Where the kernel is
+    HBM-bound the working set exceeds the 129 MB L2, yet a full ncu capture of
+    one launch ends in seconds (a few hundred MB on the device at most)."""
+    import torch
+    from thesis_gb300 import build, lib, stencil as S
+    build.build()
+    J = lib.MODE_JACOBI
+
+    def cube(n, seed=1):
+        u = S.init_uniform((n, n, n), seed)
+        return u.clone(), u.clone()
+
+    if case in ("stream_r1", "stream_r4", "stream_r1_512", "stream_r4_512"):
+        # one launch per sweep of the stream kernel
+        R = 1 if case.startswith("stream_r1") else 4
+        a, b = cube(512 if case.endswith("_512") else 320)
+        for _ in range(4):
+            S.sweep(a, b, R, 2, J, "smem_register")
+    elif case in ("persist_r1_512", "persist_r4_512"):
+        # the persistent engine AUTO runs: 8 sweeps in one cooperative launch
+        a, b = cube(512)
+        for _ in range(3):
+            S.sweep(a, b, 1 if case == "persist_r1_512" else 4, 8, J, "coop", temporal=1)
+    elif case in ("tb_r1_t2", "tb_r1_t3", "tb_r1_t4"):
+        # 3-D temporal blocking, T sweeps per HBM pass, one pass per launch
+        T = int(case[-1])
+        a, b = cube(320)
+        for _ in range(4):
+            S.sweep(a, b, 1, T, J, "coop", temporal=T)
+    elif case in ("base_r1", "tile_r1", "rows3d_r1"):
+        # base: float4 chunks through L1/L2; tile: TMA box tile with halo
+        # (smem / smem_padded roles); rows3d: full-width row slabs by bulk copy
+        a, b = cube(512 if case == "rows3d_r1" else 320)
+        variant, block = {"base_r1": ("base", (0, 0, 0)), "tile_r1": ("smem_padded", (0, 0, 0)),
+                          "rows3d_r1": ("smem_register", (0, 8, 1))}[case]
+        for _ in range(4):
+            S.sweep(a, b, 1, 2, J, variant, block=block)
+    elif case == "rows2d_8192":
+        # the persistent 2-D rows engine (grid barrier per sweep), 256 MB per buffer
+        u = S.init_uniform((8192, 8192), 1)
+        a, b = u.clone(), u.clone()
+        for _ in range(3):
+            S.sweep(a, b, 1, 8, J, "coop")
+    elif case == "cluster_2d256":
+        u = S.init_uniform((256, 256), 1)
+        a, b = u.clone(), u.clone()
+        for _ in range(4):
+            S.sweep(a, b, 1, 1000, J, "cluster")
+    elif case == "tb2d_256":
+        # the 2-D temporally blocked engine AUTO runs on 256^2, 1000 sweeps per launch
+        u = S.init_uniform((256, 256), 1)
+        a, b = u.clone(), u.clone()
+        for _ in range(4):
+            S.sweep(a, b, 1, 1000, J, "auto")
+    elif case == "ir2d_512":
+        # the persistent 2-D refinement engine: outer steps of 500 FP16 correction
+        # sweeps on the 512^2 Laplace problem
+        u = S.init_laplace2d((512, 512), 3)
+        ws = S.ir_workspace((512, 512), 1, "fp16")
+        for _ in range(3):
+            S.ir_solve_ex(u, 1, 1000, "fp16", inner_sweeps=500, workspace=ws)
+    elif case in ("ir_r1", "ir_r2", "ir_r4"):
+        # mixed-precision refinement, 512^3, 100 sweeps in outer steps of 50
+        R = int(case[-1])
+        u = S.init_fourier((512, 512, 512), 1, R)
+        for _ in range(2):
+            S.ir_solve(u, R, 100, "bf16", inner_sweeps=50)
+    elif case == "lp_sweep_r4":
+        u = S.init_fourier((384, 384, 384), 1, 4)
+        for _ in range(2):
+            S.ir_solve(u, 4, 8, "bf16", inner_sweeps=8)
+    elif case in ("conv_tc", "conv_mma"):
+        # one U-Net layer shape (d2a: 32^2, 384 -> 128 channels, batch 64) on each engine
+        from thesis_gb300 import unet as U
+        L = U._L()
+        x = torch.randn(64, 32, 32, 384, device="cuda").to(torch.bfloat16)
+        w = (torch.randn(128, 9, 384, device="cuda") * 0.05).to(torch.bfloat16)
+        bias = torch.zeros(128, device="cuda")
+        y = torch.empty(64, 32, 32, 128, dtype=torch.bfloat16, device="cuda")
+        eng = 1 if case == "conv_tc" else 2
+        for _ in range(4):
+            U._chk(L.unet_conv3x3_fwd_engine(ctypes.byref(U.view(x)), U._p(w), U._p(bias),
+                                             ctypes.byref(U.view(y)), 1, 1, eng, None), case)
+    elif case == "unet_train":
+        from thesis_gb300 import warmstart as W
+        from thesis_gb300.unet import UNet
+        fields = W.borders(range(64), 128)
+        target = W.coons_fill(fields)
+        net = UNet(seed=0)
+        for _ in range(3):
+            net.zero_grad()
+            B = net.loss_and_grad(fields, target)
+            net.backward(B)
+            net.adam_step()
+    elif case == "batch_small":
+        jobs = []
+        for k in range(64):
+            n = 64 + 32 * (k % 8)
+            u = S.init_uniform((n, n), k)
+            jobs.append((u, u.clone(), 1, 200 + 10 * k, J))
+        bt = S.Batch(jobs)
+        for _ in range(3):
+            bt.launch()
+    elif case == "batch_3d_small":
+        # the cluster phase of the benchmark batch's small 3-D part: 18 grids
+        # of 56^3 .. 104^3, R = 2, 100 sweeps each, swept from L2 by clusters
+        sides = [56 + 8 * (k % 7) for k in range(18)]
+        jobs = []
+        for k, n in enumerate(sides):
+            u = S.init_uniform((n, n, n), k)
+            jobs.append((u, u.clone(), 2, 100, J))
+        bt = S.Batch(jobs)
+        for _ in range(3):
+            bt.launch()
+        cells = sum((n - 4) ** 3 * 100 for n in sides)
+        best = 1e30
+        for _ in range(5):
+            e0, e1 = _events(torch)
+            e0.record()
+            bt.launch()
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        print("batch_3d_small: %.3f ms, %.1f GCell-updates/s" % (best, cells / best / 1e6))
+    else:
+        raise SystemExit("unknown profile case " + case)
+    torch.cuda.synchronize()
+    print("done", case)
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        _profile_case(args.profile_case)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

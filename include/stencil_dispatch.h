@@ -201,14 +201,26 @@ STENCIL_API int stencil_batch_forget(const void *d_workspace);
  * the solve stops once the relative residual (stencil_residual, computed on
  * the GPU every check_every outer steps) drops below tol.  Needs p->mode == JACOBI and
  * nx % 8 == 0; d_u's border band is never written.  Allocates nothing: the
- * caller passes a 256-byte aligned workspace of stencil_ir_workspace_bytes. */
+ * caller passes a 256-byte aligned workspace of stencil_ir_workspace_bytes.
+ * Engines: 2-D grids of at most one tile per SM (R = 1, 2, 4) run each outer
+ * step as one cooperative launch with every correction sweep in shared
+ * memory (PERSISTENT_2D); other grids launch each correction sweep
+ * (LAUNCHES).  Both give bit-identical results. */
 enum { STENCIL_STORAGE_FP32 = 0, STENCIL_STORAGE_BF16 = 1, STENCIL_STORAGE_FP16 = 2 };
+enum {
+    STENCIL_IR_ENGINE_AUTO = 0,          /* PERSISTENT_2D where it applies, else LAUNCHES */
+    STENCIL_IR_ENGINE_LAUNCHES = 1,      /* residual, sweeps and update as separate launches */
+    STENCIL_IR_ENGINE_PERSISTENT_2D = 2  /* one cooperative launch per outer step (2-D only) */
+};
 
 typedef struct stencil_ir_params {
     int storage;       /* STENCIL_STORAGE_BF16 or STENCIL_STORAGE_FP16 */
     int inner_sweeps;  /* correction sweeps per outer step (0 = 50) */
     int check_every;   /* outer steps between residual checks when tol > 0 */
-    int reserved[3];   /* must be zero */
+    int engine;        /* STENCIL_IR_ENGINE_* */
+    int temporal;      /* PERSISTENT_2D: sweeps per halo exchange (0 = chosen) */
+    int tile_x, tile_y; /* PERSISTENT_2D: owned tile in cells (0 = chosen; tile_x % 8 == 0) */
+    int reserved;      /* must be zero */
     double tol;        /* stop at this relative residual (0 = run all sweeps) */
 } stencil_ir_params;
 
@@ -216,6 +228,9 @@ typedef struct stencil_ir_result {
     int sweeps;          /* sweeps performed */
     int outer_steps;     /* refinement steps performed */
     double rel_residual; /* relative residual of the final u (stencil_residual) */
+    int engine;          /* STENCIL_IR_ENGINE_LAUNCHES or _PERSISTENT_2D: the one that ran */
+    int kernel_launches; /* kernels launched (residual checks included) */
+    int temporal, tile_x, tile_y; /* PERSISTENT_2D: the plan that ran (else 0) */
 } stencil_ir_result;
 
 STENCIL_API int stencil_ir_workspace_bytes(const stencil_params *p, const stencil_ir_params *ir,
@@ -232,9 +247,29 @@ STENCIL_API int stencil_ir_solve(const stencil_params *p, const stencil_ir_param
  * (exact wherever neighbour and centre are within a factor of two, so it
  * stays accurate relative to itself as it shrinks); FP64 is used for the
  * sums of squares only.  Agrees with an all-FP64 evaluation to about 1e-7
- * relative.  Synchronises `stream`. */
+ * relative.  d_u must be 16-byte aligned (STENCIL_EINVAL otherwise; cudaMalloc
+ * gives 256).  Synchronises `stream`. */
 STENCIL_API int stencil_residual(const stencil_params *p, const float *d_u, double *rel_residual,
                      stencil_stream_t stream);
+
+/* The plain sweep loop run to a tolerance (no counterpart in the reference,
+ * whose loop runs a fixed ITERATIONS, src/stencil_dispatch.cu:153-157): from
+ * d_u1, chunks of check_every sweeps of p (JACOBI) on the engine
+ * stencil_dispatch_ex picks, the relative residual (stencil_residual) before
+ * the first chunk and after each one, until it is below tol or p->iterations
+ * sweeps are done.  Both buffers keep the JACOBI contract (equal border
+ * bands); result->d_result is the one holding the final state.  Synchronises
+ * `stream` at every check. */
+typedef struct stencil_solve_result {
+    int sweeps;          /* sweeps performed */
+    int checks;          /* residual evaluations */
+    double rel_residual; /* relative residual of the final state */
+    float *d_result;     /* d_u1 or d_u2 */
+} stencil_solve_result;
+
+STENCIL_API int stencil_solve(const stencil_params *p, float *d_u1, float *d_u2, double tol,
+                              int check_every, stencil_stream_t stream,
+                              stencil_solve_result *result);
 
 /* Same result as stencil_residual, for callers that must not allocate device
  * memory -- e.g. a process whose own pool allocator already owns all free
@@ -243,10 +278,14 @@ STENCIL_API int stencil_residual(const stencil_params *p, const float *d_u, doub
  * reference.  Allocates nothing: its scratch is a fixed 262,160-byte device
  * array inside the library (kept on every GPU that loads it until exit), so
  * grids with more than 2^30 update cells are rejected with STENCIL_EINVAL.
- * The first call on each device looks up that array's address; make it before
- * any stream capture begins.  Calls share the array: calls that can overlap on
- * one GPU (two streams, two host threads) race and must be serialised.
- * Synchronises `stream`. */
+ * The array is reserved when the CUDA runtime loads the library's module on a
+ * device (its first kernel launch or symbol lookup under the default lazy
+ * loading; context creation with CUDA_MODULE_LOADING=EAGER), never by this
+ * call; each call looks up its address on the current device.  Calls share
+ * the array: calls that can overlap on one GPU (two streams, two host
+ * threads) race and must be serialised.  d_u must be 16-byte aligned
+ * (STENCIL_EINVAL otherwise).  Synchronises `stream`, so it cannot be
+ * captured into a CUDA graph. */
 STENCIL_API int stencil_residual_noalloc(const stencil_params *p, const float *d_u,
                                          double *rel_residual, stencil_stream_t stream);
 
@@ -288,7 +327,9 @@ STENCIL_API int stencil_tuning_set(const stencil_params *key, const stencil_para
 STENCIL_API int stencil_tuning_get(const stencil_params *key, stencil_params *choice);
 STENCIL_API int stencil_tuning_clear(void);
 
-/* Frees every workspace this library holds on the current device. */
+/* Frees every workspace this library holds on the current device.  Call it
+ * before cudaDeviceReset(): the library keeps device pointers to its
+ * workspaces between calls, and a reset leaves them dangling. */
 STENCIL_API int stencil_release(void);
 
 /* Library version and the compute capability it was built for (103). */

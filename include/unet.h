@@ -112,6 +112,21 @@ UNET_API int unet_adam(float *p, const float *g, float *m, float *v, void *p_bf1
  * band (fields is read for the border). */
 UNET_API int unet_assemble(const float *fields, const float *coons, const float *out, int n, int h,
                            int w, float *u, stencil_stream_t stream);
+/* Transfinite (Coons) interpolation of each field's border band (width 1)
+ * on its interior, the border copied: fields and u fp32 [n][h][w]. */
+UNET_API int unet_coons_fill(const float *fields, int n, int h, int w, float *u,
+                             stencil_stream_t stream);
+/* Coarse problems for the network: coarse fp32 [n][h][w] takes, on its border
+ * band, the value of fields (fp32 [n][H][W]) at the nearest fine position
+ * round(k (H-1)/(h-1)) (ties up) per axis, and zero inside. */
+UNET_API int unet_resample_border(const float *fields, int n, int H, int W, int h, int w,
+                                  float *coarse, stencil_stream_t stream);
+/* Fine initial fields from coarse predictions: u fp32 [n][H][W] is the
+ * bilinear interpolation of coarse (fp32 [n][h][w]) with corner cells
+ * aligned (fine index I at coarse position I (w-1)/(W-1)) on the interior,
+ * and equals fields (fp32 [n][H][W]) on the border band. */
+UNET_API int unet_upsample_bilinear(const float *coarse, int n, int h, int w, const float *fields,
+                                    int H, int W, float *u, stencil_stream_t stream);
 /* FP32 -> BF16 copy (count elements). */
 UNET_API int unet_to_bf16(const float *src, void *dst, long long count, stencil_stream_t stream);
 

@@ -124,6 +124,8 @@ def test_network_gradients_match_cpu_reference(cuda):
     loss = R.masked_mse(torch, out, torch.from_numpy(coons), target.cpu().double())
     loss.backward()
     # the library accumulates the sum of squares; the reference returns the mean
+    loss_rel = abs(loss_gpu / (n * (h - 2) * (w - 2)) - loss.item()) / abs(loss.item())
+    print("loss relative error %.3e" % loss_rel)
     assert loss_gpu / (n * (h - 2) * (w - 2)) == pytest.approx(loss.item(), rel=5e-2)
     worst = 0.0
     for name, _, _ in R.LAYERS:
@@ -133,6 +135,7 @@ def test_network_gradients_match_cpu_reference(cuda):
                 ref = ref.reshape(got.shape)
             rel = (got - ref).norm().item() / max(ref.norm().item(), 1e-30)
             worst = max(worst, rel)
+            print("gradient %s.%s normwise error %.3e" % (name, k, rel))
             assert rel < 0.1, (name, k, rel)
     print("worst normwise gradient error %.3e" % worst)
     for k, ref in (("dw", hw.grad), ("db", hb.grad)):

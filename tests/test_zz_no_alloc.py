@@ -4,8 +4,10 @@ Such callers -- a process whose pool allocator already owns all free device
 memory, or a latency-critical loop where cudaMalloc/cudaFree and their
 device-wide synchronisation are not allowed -- get the same answer as
 stencil_residual without the library allocating anything: the scratch lives in
-a fixed device array inside the library.  This file is named so that pytest
-collects it last.
+a fixed device array inside the library.  The array is reserved when the
+CUDA runtime loads the library's module, so the calls themselves leave the
+device's free memory unchanged.  This file is named so that pytest collects it
+last.
 """
 import ctypes
 
@@ -67,3 +69,32 @@ def test_noalloc_rejects_grids_beyond_its_fixed_scratch(stencil_lib):
     assert rc == L.EINVAL
     assert b"at most" in stencil_lib.stencil_last_error()
     assert stencil_lib.stencil_params_check(ctypes.byref(p)) == L.OK
+
+
+@pytest.mark.gpu
+def test_noalloc_leaves_free_device_memory_unchanged(cuda):
+    """After a first call (module loaded), further calls on a large grid leave
+    cudaMemGetInfo's free bytes exactly as they were."""
+    import torch
+    from thesis_gb300 import stencil as S
+    u = S.init_uniform((384, 384, 384), 9)
+    p = L.make_params(tuple(u.shape), 1, 0)
+    want = _noalloc(p, u)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(5):
+        assert _noalloc(p, u) == want
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
+def test_residual_entry_points_reject_misaligned_grids(stencil_lib):
+    """A grid pointer that is not 16-byte aligned (e.g. a sub-view one float
+    in) is refused before any launch: the kernels read 16-byte vectors."""
+    p = L.make_params((64, 64), 1, 0)
+    out = ctypes.c_double()
+    for name in ("stencil_residual_noalloc", "stencil_residual"):
+        rc = getattr(stencil_lib, name)(ctypes.byref(p), ctypes.c_void_p(4096 + 4),
+                                        ctypes.byref(out), None)
+        assert rc == L.EINVAL, name
+        assert b"16-byte aligned" in stencil_lib.stencil_last_error()

@@ -462,6 +462,8 @@ int stencil_residual(const stencil_params *p, const float *d_u, double *rel_resi
     int rc = stencil_params_check(p);
     if (rc) return rc;
     if (!d_u || !rel_residual) return fail(STENCIL_EINVAL, "null pointer");
+    if (reinterpret_cast<uintptr_t>(d_u) & 15)
+        return fail(STENCIL_EINVAL, "d_u must be 16-byte aligned (the kernels read 16-byte vectors)");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     void *scratch = nullptr;
     {
@@ -478,6 +480,41 @@ int stencil_residual(const stencil_params *p, const float *d_u, double *rel_resi
         ST_CUDA(cudaStreamSynchronize(s));
         *rel_residual = sums[1] > 0.0 ? sqrt(sums[0]) / sqrt(sums[1]) : sqrt(sums[0]);
     }
+    return STENCIL_OK;
+}
+
+int stencil_solve(const stencil_params *p, float *d_u1, float *d_u2, double tol, int check_every,
+                  stencil_stream_t stream, stencil_solve_result *result) {
+    int rc = stencil_params_check(p);
+    if (rc) return rc;
+    if (!result) return fail(STENCIL_EINVAL, "null result");
+    if (p->mode != STENCIL_MODE_JACOBI) return fail(STENCIL_EINVAL, "a tolerance needs JACOBI sweeps");
+    if (check_every < 1 || !(tol >= 0.0)) return fail(STENCIL_EINVAL, "check_every >= 1 and tol >= 0");
+    float *cur = d_u1, *nxt = d_u2;
+    stencil_params q = *p;
+    double rel = 0.0;
+    int done = 0, checks = 0;
+    rc = stencil_residual(p, cur, &rel, stream);
+    if (rc) return rc;
+    ++checks;
+    long long launches = 0;
+    while (rel >= tol && done < p->iterations) {
+        q.iterations = std::min(check_every, p->iterations - done);
+        float *res = nullptr;
+        rc = stencil_dispatch_ex(&q, cur, nxt, stream, &res);
+        if (rc) return rc;
+        launches += t_launches;
+        if (res != cur) std::swap(cur, nxt);
+        done += q.iterations;
+        rc = stencil_residual(p, cur, &rel, stream);
+        if (rc) return rc;
+        ++checks;
+    }
+    t_launches = launches + 2LL * checks;
+    result->sweeps = done;
+    result->checks = checks;
+    result->rel_residual = rel;
+    result->d_result = cur;
     return STENCIL_OK;
 }
 

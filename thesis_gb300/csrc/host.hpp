@@ -80,6 +80,28 @@ bool cluster_resident(const Geom &g, int dims);
 // fewer than 2^31 float4 chunks).
 bool cluster_shape_ok(int dims, int nx, int ny, int radius);
 
+// Mixed-precision refinement, persistent 2-D form of an outer step
+// (k_ir2d.cu): one CTA per tile, T correction sweeps per halo exchange.
+struct Ir2Plan {
+    int tx, ty;          // owned tile (cells); tx % 8 == 0
+    int t;               // sweeps per exchange
+    int hx, hy;          // halo: x in whole 8-cell chunks, y = t * R
+    int pw, ph;          // grown tile (pw % 8 == 0)
+    int tiles_x, tiles_y;
+};
+// Exchange-buffer bytes any plan of the grid needs.
+size_t ir2_xch_bytes(const Geom &g);
+// A plan for outer steps of m sweeps (temporal / tile_* 0 = chosen); false
+// if the grid does not fit one tile per SM.  E = __nv_bfloat16 or __half.
+template <typename E>
+bool ir2_plan(const Geom &g, int m, int temporal, int tile_x, int tile_y, Ir2Plan *p);
+// One outer step of m sweeps on u.  The counters (bar, the two max_bits
+// words) and the exchange buffer are zeroed once per solve; step counts the
+// launches since then and tag0 grows by m + 1 per launch.
+template <typename E>
+int ir2_launch(const Geom &g, const Ir2Plan &p, float *u, unsigned long long *xch, unsigned *bar,
+               unsigned *max_bits, float *scale, int step, unsigned tag0, int m, cudaStream_t s);
+
 // Plain whole-grid helpers.
 int launch_copy_border(const Geom &g, int dims, const float *src, float *dst, cudaStream_t s);
 int launch_init_reference(const Geom &g, int dims, float *u, cudaStream_t s);

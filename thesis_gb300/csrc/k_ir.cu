@@ -15,6 +15,9 @@
 // tolerance is given.  Correction sweeps move 6 bytes per cell update (read e
 // and r, write e) instead of 8; on 3-D grids they run on the TMA-fed stream
 // form (k_lpstream.cu), elsewhere on k_lp_sweep below (the same arithmetic).
+// 2-D grids of at most one tile per SM run each outer step as one
+// cooperative launch instead (k_ir2d.cu: every correction sweep on chip,
+// bit-identical to the launches here).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -90,11 +93,14 @@ __global__ void __launch_bounds__(256)
             unpack8<E>(__ldg(src + v), w + 8);
             unpack8<E>(v + 1 < nv ? __ldg(src + v + 1) : z4, w + 16);
         }
+        // the sum starts from its first term, as in the persistent 2-D form
+        // (k_ir2d.cu) and the 3-D stream form (a sum started from +0 differs
+        // only when every term is -0: +0 there, -0 here)
         float acc[8];
 #pragma unroll
-        for (int c = 0; c < 8; ++c) acc[c] = 0.0f;
+        for (int c = 0; c < 8; ++c) acc[c] = w[8 + c - R];
 #pragma unroll
-        for (int o = -R; o <= R; ++o) {
+        for (int o = -R + 1; o <= R; ++o) {
             if (!o) continue;
 #pragma unroll
             for (int c = 0; c < 8; ++c) acc[c] += w[8 + c + o];
@@ -267,56 +273,119 @@ __global__ void __launch_bounds__(256)
 
 namespace {
 
+// Workspace layout: r, e_a, e_b (16-bit grids), a 256-byte block of
+// counters, the residual scratch, and for 2-D grids the exchange buffer of
+// the persistent form.
+struct IrLayout {
+    size_t lp, ctl, resid, xch, total;
+};
+
+IrLayout ir_layout(const stencil_params &p, int storage) {
+    const size_t n = (size_t)cell_count(p);
+    const size_t esz = storage == STENCIL_STORAGE_FP32 ? 4 : 2;
+    IrLayout l;
+    l.lp = (n * esz + 255) & ~(size_t)255;
+    l.ctl = 3 * l.lp;
+    l.resid = l.ctl + 256;
+    l.xch = (l.resid + residual_scratch_bytes() + 255) & ~(size_t)255;
+    l.total = l.xch + (p.dims == 2 ? ir2_xch_bytes(make_geom(p)) : 0);
+    return l;
+}
+
+// Relative residual of u into *rel (synchronises s).
+int ir_check(const Geom &g, int dims, const float *u, double *resid, cudaStream_t s, double *rel) {
+    int rc = launch_residual(g, dims, u, resid, s);
+    if (rc) return rc;
+    double sums[2];
+    const size_t off = residual_scratch_bytes() / sizeof(double) - 2;
+    ST_CUDA(cudaMemcpyAsync(sums, resid + off, sizeof sums, cudaMemcpyDeviceToHost, s));
+    ST_CUDA(cudaStreamSynchronize(s));
+    *rel = sums[1] > 0.0 ? sqrt(sums[0]) / sqrt(sums[1]) : sqrt(sums[0]);
+    return STENCIL_OK;
+}
+
 template <typename E, int D, int R>
 int ir_loop(const stencil_params &p, const stencil_ir_params &ir, float *u, char *ws,
             cudaStream_t s, stencil_ir_result *out) {
     const Geom g = make_geom(p);
     const size_t n = (size_t)cell_count(p);
-    const size_t lp_bytes = (n * sizeof(E) + 255) & ~(size_t)255;
+    const IrLayout L = ir_layout(p, ir.storage);
     E *r = reinterpret_cast<E *>(ws);
-    E *ea = reinterpret_cast<E *>(ws + lp_bytes);
-    E *eb = reinterpret_cast<E *>(ws + 2 * lp_bytes);
-    unsigned *max_bits = reinterpret_cast<unsigned *>(ws + 3 * lp_bytes);
-    float *scale = reinterpret_cast<float *>(ws + 3 * lp_bytes + 4);
-    double *resid = reinterpret_cast<double *>(ws + 3 * lp_bytes + 256);
-    // Border bands of r and e stay zero for the whole solve.
-    ST_CUDA(cudaMemsetAsync(ws, 0, 3 * lp_bytes, s));
-    const int blocks = 4 * num_sms();
+    E *ea = reinterpret_cast<E *>(ws + L.lp);
+    E *eb = reinterpret_cast<E *>(ws + 2 * L.lp);
+    unsigned *max_bits = reinterpret_cast<unsigned *>(ws + L.ctl);
+    float *scale = reinterpret_cast<float *>(ws + L.ctl + 4);
+    unsigned *max2 = reinterpret_cast<unsigned *>(ws + L.ctl + 16);  // two words
+    unsigned *bar2 = reinterpret_cast<unsigned *>(ws + L.ctl + 32);
+    double *resid = reinterpret_cast<double *>(ws + L.resid);
+    unsigned long long *xch = reinterpret_cast<unsigned long long *>(ws + L.xch);
     const int m_inner = ir.inner_sweeps > 0 ? ir.inner_sweeps : 50;
-    int done = 0, outer = 0;
+    Ir2Plan plan = {};
+    const bool persistent = D == 2 && ir.engine != STENCIL_IR_ENGINE_LAUNCHES &&
+                            ir2_plan<E>(g, m_inner, ir.temporal, ir.tile_x, ir.tile_y, &plan);
+    if (ir.engine == STENCIL_IR_ENGINE_PERSISTENT_2D && !persistent)
+        return fail(STENCIL_EUNSUPPORTED,
+                    "the persistent refinement engine takes 2-D grids of at most one tile per SM "
+                    "with R = 1, 2 or 4");
+    if (persistent) {
+        ST_CUDA(cudaMemsetAsync(ws + L.ctl, 0, 256, s));
+        ST_CUDA(cudaMemsetAsync(xch, 0, ir2_xch_bytes(g), s));
+    } else {
+        // Border bands of r and e stay zero for the whole solve.
+        ST_CUDA(cudaMemsetAsync(ws, 0, 3 * L.lp, s));
+    }
+    const int blocks = 4 * num_sms();
+    int done = 0, outer = 0, step = 0;
+    unsigned tag0 = 0;
+    long long launches = 0;
     double rel = -1.0;
     while (done < p.iterations) {
         const int m = std::min(m_inner, p.iterations - done);
-        ST_CUDA(cudaMemsetAsync(max_bits, 0, sizeof(unsigned), s));
-        k_ir_resid<E, D, R><<<blocks, 256, 0, s>>>(u, r, g, max_bits, scale, 0);
-        k_ir_resid<E, D, R><<<blocks, 256, 0, s>>>(u, r, g, max_bits, scale, 1);
-        ST_CUDA(cudaGetLastError());
-        ST_CUDA(cudaMemcpyAsync(ea, r, n * sizeof(E), cudaMemcpyDeviceToDevice, s));
-        E *cur = ea, *nxt = eb;
-        const bool streamed = lp_stream_supported(g, D);
-        for (int it = 1; it < m; ++it) {
-            if (streamed) {
-                int rc = launch_lp_stream<E>(g, cur, nxt, r, s);
-                if (rc) return rc;
-            } else {
-                k_lp_sweep<E, D, R><<<8 * num_sms(), 256, 0, s>>>(cur, nxt, r, g);
+        if (persistent) {
+            // counters grow monotonically within a solve; restart them before
+            // they could wrap
+            const unsigned grid = (unsigned)(plan.tiles_x * plan.tiles_y);
+            if ((unsigned long long)(step + 2) * grid >= 0xffffffffull ||
+                (unsigned long long)tag0 + (unsigned)m + 2 >= 0xffffffffull) {
+                ST_CUDA(cudaMemsetAsync(ws + L.ctl, 0, 256, s));
+                ST_CUDA(cudaMemsetAsync(xch, 0, ir2_xch_bytes(g), s));
+                step = 0;
+                tag0 = 0;
             }
-            std::swap(cur, nxt);
+            int rc = ir2_launch<E>(g, plan, u, xch, bar2, max2, scale, step, tag0, m, s);
+            if (rc) return rc;
+            ++step;
+            tag0 += (unsigned)m + 1;
+            ++launches;
+        } else {
+            ST_CUDA(cudaMemsetAsync(max_bits, 0, sizeof(unsigned), s));
+            k_ir_resid<E, D, R><<<blocks, 256, 0, s>>>(u, r, g, max_bits, scale, 0);
+            k_ir_resid<E, D, R><<<blocks, 256, 0, s>>>(u, r, g, max_bits, scale, 1);
+            ST_CUDA(cudaGetLastError());
+            ST_CUDA(cudaMemcpyAsync(ea, r, n * sizeof(E), cudaMemcpyDeviceToDevice, s));
+            E *cur = ea, *nxt = eb;
+            const bool streamed = lp_stream_supported(g, D);
+            for (int it = 1; it < m; ++it) {
+                if (streamed) {
+                    int rc = launch_lp_stream<E>(g, cur, nxt, r, s);
+                    if (rc) return rc;
+                } else {
+                    k_lp_sweep<E, D, R><<<8 * num_sms(), 256, 0, s>>>(cur, nxt, r, g);
+                }
+                std::swap(cur, nxt);
+            }
+            ST_CUDA(cudaGetLastError());
+            k_ir_update<E, D, R><<<blocks, 256, 0, s>>>(u, cur, g, scale);
+            ST_CUDA(cudaGetLastError());
+            launches += 3 + (m - 1);
         }
-        ST_CUDA(cudaGetLastError());
-        k_ir_update<E, D, R><<<blocks, 256, 0, s>>>(u, cur, g, scale);
-        ST_CUDA(cudaGetLastError());
         done += m;
         ++outer;
         const bool last = done >= p.iterations;
         if ((ir.tol > 0.0 && (ir.check_every <= 1 || outer % ir.check_every == 0)) || last) {
-            int rc = launch_residual(g, p.dims, u, resid, s);
+            int rc = ir_check(g, p.dims, u, resid, s, &rel);
             if (rc) return rc;
-            double sums[2];
-            const size_t off = residual_scratch_bytes() / sizeof(double) - 2;
-            ST_CUDA(cudaMemcpyAsync(sums, resid + off, sizeof sums, cudaMemcpyDeviceToHost, s));
-            ST_CUDA(cudaStreamSynchronize(s));
-            rel = sums[1] > 0.0 ? sqrt(sums[0]) / sqrt(sums[1]) : sqrt(sums[0]);
+            launches += 2;
             if (ir.tol > 0.0 && rel < ir.tol) break;
         }
     }
@@ -324,6 +393,11 @@ int ir_loop(const stencil_params &p, const stencil_ir_params &ir, float *u, char
         out->sweeps = done;
         out->outer_steps = outer;
         out->rel_residual = rel;
+        out->engine = persistent ? STENCIL_IR_ENGINE_PERSISTENT_2D : STENCIL_IR_ENGINE_LAUNCHES;
+        out->kernel_launches = (int)std::min<long long>(launches, 0x7fffffff);
+        out->temporal = persistent ? plan.t : 0;
+        out->tile_x = persistent ? plan.tx : 0;
+        out->tile_y = persistent ? plan.ty : 0;
     }
     return STENCIL_OK;
 }
@@ -343,12 +417,7 @@ int ir_dispatch(const stencil_params &p, const stencil_ir_params &ir, float *u, 
     }
 }
 
-size_t ir_bytes(const stencil_params &p, int storage) {
-    const size_t n = (size_t)cell_count(p);
-    const size_t esz = storage == STENCIL_STORAGE_FP32 ? 4 : 2;
-    const size_t lp = (n * esz + 255) & ~(size_t)255;
-    return 3 * lp + 256 + residual_scratch_bytes();
-}
+size_t ir_bytes(const stencil_params &p, int storage) { return ir_layout(p, storage).total; }
 
 }  // namespace
 }  // namespace st
@@ -374,10 +443,13 @@ extern "C" int stencil_ir_solve(const stencil_params *p, const stencil_ir_params
         return fail(STENCIL_EINVAL, "iterative refinement solves the JACOBI steady state");
     if (ir->storage != STENCIL_STORAGE_BF16 && ir->storage != STENCIL_STORAGE_FP16)
         return fail(STENCIL_EINVAL, "storage must be STENCIL_STORAGE_BF16 or STENCIL_STORAGE_FP16");
-    if (ir->inner_sweeps < 0 || ir->check_every < 0 || ir->tol < 0.0)
-        return fail(STENCIL_EINVAL, "inner_sweeps, check_every and tol must be >= 0");
-    for (int r : ir->reserved)
-        if (r) return fail(STENCIL_EINVAL, "reserved fields must be zero");
+    if (ir->inner_sweeps < 0 || ir->check_every < 0 || ir->tol < 0.0 || ir->temporal < 0 ||
+        ir->tile_x < 0 || ir->tile_y < 0)
+        return fail(STENCIL_EINVAL,
+                    "inner_sweeps, check_every, temporal, tile_x, tile_y and tol must be >= 0");
+    if (ir->engine < STENCIL_IR_ENGINE_AUTO || ir->engine > STENCIL_IR_ENGINE_PERSISTENT_2D)
+        return fail(STENCIL_EINVAL, "engine must be a STENCIL_IR_ENGINE_* value");
+    if (ir->reserved) return fail(STENCIL_EINVAL, "reserved fields must be zero");
     if (p->nx % 8) return fail(STENCIL_EUNSUPPORTED, "IR needs nx %% 8 == 0");
     if (workspace_bytes < ir_bytes(*p, ir->storage))
         return fail(STENCIL_EINVAL, "workspace too small (%zu < %zu bytes)", workspace_bytes,

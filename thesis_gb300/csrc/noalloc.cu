@@ -19,10 +19,14 @@
 // the same call.  Calls whose kernels can overlap on one GPU (calls on two
 // streams, or from two host threads) race on the array: serialise them.
 //
-// The first call on each device looks up the array's device address
-// (cudaGetSymbolAddress) with that device current; make that first call
-// before any stream capture begins.
-#include <mutex>
+// Every call looks up the array's device address (cudaGetSymbolAddress, which
+// allocates nothing) with the caller's device current, so the address stays
+// right after a cudaDeviceReset reloads the library's module.  The array is
+// reserved when the CUDA runtime loads this library's module on a device: at
+// the first kernel launch or symbol lookup under lazy module loading (the
+// default), at context creation with CUDA_MODULE_LOADING=EAGER.  The call
+// synchronises its stream, so it cannot be captured into a CUDA graph.
+#include <stdint.h>
 
 #include "host.hpp"
 
@@ -39,23 +43,13 @@ constexpr long long kNoAllocCellsPerPart = 65536;
 
 static __device__ __align__(256) double g_noalloc_scratch[2 * kNoAllocMaxParts + 2];
 
-// Device address of g_noalloc_scratch, looked up once per device with that
-// device current.  In host code the array's name is only a host-side stand-in.
-static std::mutex g_noalloc_mu;
-static double *g_noalloc_addr[64];
-
+// Device address of g_noalloc_scratch on the current device.  In host code
+// the array's name is only a host-side stand-in, never a device address.
 static int noalloc_scratch(double **out) {
-    int dev = 0;
-    ST_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) return fail(STENCIL_ENODEVICE, "device index %d out of range", dev);
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-        g_noalloc_addr[dev] = static_cast<double *>(p);
-    }
-    *out = g_noalloc_addr[dev];
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    *out = static_cast<double *>(p);
     return STENCIL_OK;
 }
 
@@ -68,6 +62,8 @@ extern "C" int stencil_residual_noalloc(const stencil_params *p, const float *d_
     int rc = stencil_params_check(p);
     if (rc) return rc;
     if (!d_u || !rel_residual) return fail(STENCIL_EINVAL, "null pointer");
+    if (reinterpret_cast<uintptr_t>(d_u) & 15)
+        return fail(STENCIL_EINVAL, "d_u must be 16-byte aligned (the kernels read 16-byte vectors)");
     const Geom g = make_geom(*p);
     const long long inner = (long long)(g.nx - 2 * g.radius) * (g.ny - 2 * g.radius) *
                             (p->dims == 3 ? g.nz - 2 * g.radius : 1);

@@ -1145,6 +1145,72 @@ __global__ void k_assemble(const float *f, const float *coons, const float *out,
     }
 }
 
+// Transfinite (Coons) interpolation of each field's border on its interior,
+// the border band copied (the formula of k_features' channel 2).
+__global__ void k_coons_fill(const float *__restrict__ f, int n, int h, int w, float *__restrict__ u) {
+    const long long P = (long long)n * h * w;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < P;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(p % w), j = (int)((p / w) % h), nn = (int)(p / ((long long)w * h));
+        const float *g = f + (long long)nn * h * w;
+        const bool bnd = i == 0 || j == 0 || i == w - 1 || j == h - 1;
+        const float s = (float)i / (w - 1), t = (float)j / (h - 1);
+        const float B = g[i], T = g[(long long)(h - 1) * w + i];
+        const float L = g[(long long)j * w], Rr = g[(long long)j * w + w - 1];
+        const float c00 = g[0], c10 = g[w - 1], c01 = g[(long long)(h - 1) * w], c11 = g[(long long)h * w - 1];
+        const float cp = (1 - t) * B + t * T + (1 - s) * L + s * Rr -
+                         ((1 - s) * (1 - t) * c00 + s * (1 - t) * c10 + (1 - s) * t * c01 + s * t * c11);
+        u[p] = bnd ? g[(long long)j * w + i] : cp;
+    }
+}
+
+// Nearest source index of coarse index k when k = 0..m-1 spans 0..M-1:
+// round(k (M-1) / (m-1)), ties up.
+__device__ __forceinline__ int nearest_index(int k, int m, int M) {
+    return m > 1 ? (int)((2LL * k * (M - 1) + (m - 1)) / (2LL * (m - 1))) : 0;
+}
+
+// Coarse h x w problems from fine H x W borders: each coarse border cell
+// takes the fine border value at the nearest position; interior zero.
+__global__ void k_resample_border(const float *__restrict__ f, int n, int H, int W, int h, int w,
+                                  float *__restrict__ c) {
+    const long long P = (long long)n * h * w;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < P;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(p % w), j = (int)((p / w) % h), nn = (int)(p / ((long long)w * h));
+        const bool bnd = i == 0 || j == 0 || i == w - 1 || j == h - 1;
+        float v = 0.0f;
+        if (bnd)
+            v = f[(long long)nn * H * W + (long long)nearest_index(j, h, H) * W + nearest_index(i, w, W)];
+        c[p] = v;
+    }
+}
+
+// Fine H x W fields from coarse h x w ones: bilinear interpolation with the
+// corner cells aligned (fine index I maps to I (w-1)/(W-1)) on the interior;
+// the fine border band is copied from f.
+__global__ void k_upsample_bilinear(const float *__restrict__ c, int n, int h, int w,
+                                    const float *__restrict__ f, int H, int W, float *__restrict__ u) {
+    const long long P = (long long)n * H * W;
+    const float sx = W > 1 ? (float)(w - 1) / (float)(W - 1) : 0.0f;
+    const float sy = H > 1 ? (float)(h - 1) / (float)(H - 1) : 0.0f;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < P;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int I = (int)(p % W), J = (int)((p / W) % H), nn = (int)(p / ((long long)W * H));
+        if (I == 0 || J == 0 || I == W - 1 || J == H - 1) {
+            u[p] = f[p];
+            continue;
+        }
+        const float x = I * sx, y = J * sy;
+        const int x0 = min((int)x, w - 2), y0 = min((int)y, h - 2);
+        const float ax = x - x0, ay = y - y0;
+        const float *g = c + (long long)nn * h * w + (long long)y0 * w + x0;
+        const float top = (1.0f - ax) * g[0] + ax * g[1];
+        const float bot = (1.0f - ax) * g[w] + ax * g[w + 1];
+        u[p] = (1.0f - ay) * top + ay * bot;
+    }
+}
+
 __global__ void k_to_bf16(const float *s, bf16 *d, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x)
@@ -1499,6 +1565,29 @@ extern "C" int unet_assemble(const float *fields, const float *coons, const floa
     if (!fields || !coons || !out || !u) return fail(STENCIL_EINVAL, "null pointer");
     k_assemble<<<grid_for((long long)n * h * w), 256, 0, STREAM(s)>>>(fields, coons, out, n, h, w, u);
     return cuda_fail(cudaGetLastError(), "assemble launch");
+}
+
+extern "C" int unet_coons_fill(const float *fields, int n, int h, int w, float *u, stencil_stream_t s) {
+    if (!fields || !u || n < 0 || h < 2 || w < 2) return fail(STENCIL_EINVAL, "bad arguments");
+    k_coons_fill<<<grid_for((long long)n * h * w), 256, 0, STREAM(s)>>>(fields, n, h, w, u);
+    return cuda_fail(cudaGetLastError(), "coons_fill launch");
+}
+
+extern "C" int unet_resample_border(const float *fields, int n, int H, int W, int h, int w,
+                                    float *coarse, stencil_stream_t s) {
+    if (!fields || !coarse || n < 0 || H < 2 || W < 2 || h < 2 || w < 2)
+        return fail(STENCIL_EINVAL, "bad arguments");
+    k_resample_border<<<grid_for((long long)n * h * w), 256, 0, STREAM(s)>>>(fields, n, H, W, h, w, coarse);
+    return cuda_fail(cudaGetLastError(), "resample_border launch");
+}
+
+extern "C" int unet_upsample_bilinear(const float *coarse, int n, int h, int w, const float *fields,
+                                      int H, int W, float *u, stencil_stream_t s) {
+    if (!coarse || !fields || !u || n < 0 || H < 2 || W < 2 || h < 2 || w < 2)
+        return fail(STENCIL_EINVAL, "bad arguments");
+    k_upsample_bilinear<<<grid_for((long long)n * H * W), 256, 0, STREAM(s)>>>(coarse, n, h, w, fields, H,
+                                                                             W, u);
+    return cuda_fail(cudaGetLastError(), "upsample_bilinear launch");
 }
 
 extern "C" int unet_to_bf16(const float *src, void *dst, long long count, stencil_stream_t s) {

@@ -45,16 +45,27 @@ class BatchJob(ctypes.Structure):
 
 class IrParams(ctypes.Structure):
     _fields_ = [("storage", ctypes.c_int), ("inner_sweeps", ctypes.c_int),
-                ("check_every", ctypes.c_int), ("reserved", ctypes.c_int * 3),
-                ("tol", ctypes.c_double)]
+                ("check_every", ctypes.c_int), ("engine", ctypes.c_int),
+                ("temporal", ctypes.c_int), ("tile_x", ctypes.c_int), ("tile_y", ctypes.c_int),
+                ("reserved", ctypes.c_int), ("tol", ctypes.c_double)]
 
 
 class IrResult(ctypes.Structure):
     _fields_ = [("sweeps", ctypes.c_int), ("outer_steps", ctypes.c_int),
-                ("rel_residual", ctypes.c_double)]
+                ("rel_residual", ctypes.c_double), ("engine", ctypes.c_int),
+                ("kernel_launches", ctypes.c_int), ("temporal", ctypes.c_int),
+                ("tile_x", ctypes.c_int), ("tile_y", ctypes.c_int)]
+
+
+class SolveResult(ctypes.Structure):
+    _fields_ = [("sweeps", ctypes.c_int), ("checks", ctypes.c_int),
+                ("rel_residual", ctypes.c_double), ("d_result", ctypes.c_void_p)]
 
 
 STORAGE_FP32, STORAGE_BF16, STORAGE_FP16 = 0, 1, 2
+IR_ENGINE_AUTO, IR_ENGINE_LAUNCHES, IR_ENGINE_PERSISTENT_2D = 0, 1, 2
+IR_ENGINE_NAMES = {"auto": IR_ENGINE_AUTO, "launches": IR_ENGINE_LAUNCHES,
+                   "persistent2d": IR_ENGINE_PERSISTENT_2D}
 
 
 class StencilParams(ctypes.Structure):
@@ -97,6 +108,7 @@ def load() -> ctypes.CDLL:
         "stencil_init_laplace2d": (i, [P, vp, u64, vp]),
         "stencil_residual": (i, [P, vp, ctypes.POINTER(ctypes.c_double), vp]),
         "stencil_residual_noalloc": (i, [P, vp, ctypes.POINTER(ctypes.c_double), vp]),
+        "stencil_solve": (i, [P, vp, vp, ctypes.c_double, i, vp, ctypes.POINTER(SolveResult)]),
         "stencil_selftest_div": (i, [i, ctypes.POINTER(ctypes.c_ulonglong),
                                      ctypes.POINTER(ctypes.c_uint)]),
         "stencil_selftest_wait": (i, [i, ctypes.POINTER(i), ctypes.POINTER(i)]),

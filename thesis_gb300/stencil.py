@@ -159,6 +159,21 @@ def residual(u, radius: int, stream=None) -> float:
     return out.value
 
 
+def solve(d_u1, d_u2, radius: int, max_sweeps: int, tol: float, check_every: int = 500,
+          variant="auto", stream=None):
+    """Plain JACOBI sweeps from d_u1 to relative residual tol, checked every
+    check_every sweeps (stencil_solve).  Returns (sweeps, rel_residual,
+    buffer holding the result)."""
+    _check_tensor(d_u1)
+    _check_tensor(d_u2, d_u1.shape)
+    p = _lib.make_params(tuple(d_u1.shape), radius, max_sweeps, _lib.MODE_JACOBI, variant)
+    r = _lib.SolveResult()
+    _lib.check(_lib.load().stencil_solve(ctypes.byref(p), ctypes.c_void_p(d_u1.data_ptr()),
+                                         ctypes.c_void_p(d_u2.data_ptr()), tol, check_every,
+                                         _stream_handle(stream), ctypes.byref(r)), "stencil_solve")
+    return r.sweeps, r.rel_residual, (d_u1 if r.d_result == d_u1.data_ptr() else d_u2)
+
+
 def run_host(h_in: np.ndarray, radius: int, iterations: int, mode: int = _lib.MODE_JACOBI,
              variant="auto", block=(0, 0, 0), coarsen_x: int = 0, temporal: int = 0,
              out: np.ndarray | None = None, sweeps_ms: bool = False):
@@ -254,16 +269,32 @@ class Batch:
             self.ws = None
 
 
-def ir_solve(d_u, radius: int, iterations: int, storage: str = "bf16", inner_sweeps: int = 0,
-             tol: float = 0.0, check_every: int = 1, workspace=None, stream=None):
+def ir_workspace(shape, radius: int, storage: str = "bf16", device="cuda"):
+    """A device workspace for ir_solve on grids of this shape (reusable)."""
+    import torch
+    p = _lib.make_params(tuple(shape), radius, 0, _lib.MODE_JACOBI)
+    ir = _lib.IrParams()
+    ir.storage = {"bf16": _lib.STORAGE_BF16, "fp16": _lib.STORAGE_FP16}[storage]
+    nbytes = ctypes.c_size_t()
+    _lib.check(_lib.load().stencil_ir_workspace_bytes(ctypes.byref(p), ctypes.byref(ir),
+                                                      ctypes.byref(nbytes)),
+               "stencil_ir_workspace_bytes")
+    return torch.empty(nbytes.value + 256, dtype=torch.uint8, device=device)
+
+
+def ir_solve_ex(d_u, radius: int, iterations: int, storage: str = "bf16", inner_sweeps: int = 0,
+                tol: float = 0.0, check_every: int = 1, engine="auto", temporal: int = 0,
+                tile=(0, 0), workspace=None, stream=None) -> dict:
     """Mixed-precision iterative refinement in place on the FP32 master d_u
-    (stencil_ir_solve).  Returns (sweeps, outer_steps, rel_residual)."""
+    (stencil_ir_solve).  Returns the stencil_ir_result fields as a dict."""
     import torch
     _check_tensor(d_u)
     p = _lib.make_params(tuple(d_u.shape), radius, iterations, _lib.MODE_JACOBI)
     ir = _lib.IrParams()
     ir.storage = {"bf16": _lib.STORAGE_BF16, "fp16": _lib.STORAGE_FP16}[storage]
     ir.inner_sweeps, ir.check_every, ir.tol = inner_sweeps, check_every, tol
+    ir.engine = _lib.IR_ENGINE_NAMES[engine] if isinstance(engine, str) else engine
+    ir.temporal, ir.tile_x, ir.tile_y = temporal, tile[0], tile[1]
     L = _lib.load()
     nbytes = ctypes.c_size_t()
     _lib.check(L.stencil_ir_workspace_bytes(ctypes.byref(p), ctypes.byref(ir), ctypes.byref(nbytes)),
@@ -275,4 +306,17 @@ def ir_solve(d_u, radius: int, iterations: int, storage: str = "bf16", inner_swe
     _lib.check(L.stencil_ir_solve(ctypes.byref(p), ctypes.byref(ir), ctypes.c_void_p(d_u.data_ptr()),
                                   ctypes.c_void_p(ws), nbytes.value, _stream_handle(stream),
                                   ctypes.byref(res)), "stencil_ir_solve")
-    return res.sweeps, res.outer_steps, res.rel_residual
+    names = {_lib.IR_ENGINE_LAUNCHES: "launches", _lib.IR_ENGINE_PERSISTENT_2D: "persistent2d"}
+    return {"sweeps": res.sweeps, "outer_steps": res.outer_steps,
+            "rel_residual": res.rel_residual, "engine": names.get(res.engine, str(res.engine)),
+            "kernel_launches": res.kernel_launches, "temporal": res.temporal,
+            "tile": (res.tile_x, res.tile_y)}
+
+
+def ir_solve(d_u, radius: int, iterations: int, storage: str = "bf16", inner_sweeps: int = 0,
+             tol: float = 0.0, check_every: int = 1, workspace=None, stream=None, engine="auto"):
+    """Mixed-precision iterative refinement in place on the FP32 master d_u
+    (stencil_ir_solve).  Returns (sweeps, outer_steps, rel_residual)."""
+    r = ir_solve_ex(d_u, radius, iterations, storage, inner_sweeps, tol, check_every, engine,
+                    workspace=workspace, stream=stream)
+    return r["sweeps"], r["outer_steps"], r["rel_residual"]

@@ -78,6 +78,9 @@ def _L():
             "unet_adam": [vp, vp, vp, vp, vp, ll, f, f, f, f, i, vp],
             "unet_assemble": [vp, vp, vp, i, i, i, vp, vp],
             "unet_to_bf16": [vp, vp, ll, vp],
+            "unet_coons_fill": [vp, i, i, i, vp, vp],
+            "unet_resample_border": [vp, i, i, i, i, i, vp, vp],
+            "unet_upsample_bilinear": [vp, i, i, i, vp, i, i, vp, vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -359,6 +362,38 @@ class UNet:
         n, h, w = fields.shape
         _chk(_L().unet_assemble(_p(fields), _p(coons), _p(out), n, h, w, _p(u), s), "assemble")
         return u
+
+
+def coons_fill(fields, stream=None):
+    """Border kept, interior = transfinite interpolation of the border
+    (fields fp32 [n, h, w]; one kernel)."""
+    import torch
+    n, h, w = fields.shape
+    u = torch.empty_like(fields)
+    _chk(_L().unet_coons_fill(_p(fields), n, h, w, _p(u), _stream(stream)), "unet_coons_fill")
+    return u
+
+
+def resample_border(fields, h, w, stream=None):
+    """Coarse h x w problems: the fine border sampled at the nearest positions, zero interior."""
+    import torch
+    n, H, W = fields.shape
+    c = torch.empty((n, h, w), dtype=torch.float32, device=fields.device)
+    _chk(_L().unet_resample_border(_p(fields), n, H, W, h, w, _p(c), _stream(stream)),
+         "unet_resample_border")
+    return c
+
+
+def upsample_bilinear(coarse, fields, stream=None):
+    """Fine fields: bilinear (corners aligned) interpolation of coarse inside,
+    the fine border of `fields` on the band."""
+    import torch
+    n, h, w = coarse.shape
+    _, H, W = fields.shape
+    u = torch.empty_like(fields)
+    _chk(_L().unet_upsample_bilinear(_p(coarse), n, h, w, _p(fields), H, W, _p(u), _stream(stream)),
+         "unet_upsample_bilinear")
+    return u
 
 
 def _stream(stream):

@@ -9,12 +9,18 @@ Pipeline:
      interpolation of the border;
   2. training: the U-Net of unet.py, every kernel hand-written (BF16 tensor
      cores, FP32 accumulation), Adam on FP32 master weights;
-  3. solve: the predicted field seeds plain FP32 Jacobi, which runs to the
-     relative residual tolerance; the prediction replaces zero only when its
-     residual is lower (fallback rule).
+  3. solve: the network, applied to the border resampled to the training size,
+     predicts the initial field (bilinear back to the grid); the solver runs
+     from it to the relative residual tolerance -- plain FP32 Jacobi, or the
+     mixed-precision refinement (FP16/BF16 correction sweeps, FP32 master,
+     FP64 residual norm; stencil_ir_solve) -- and the prediction replaces zero
+     only when its residual is lower (fallback rule).
 
-The sweep counts to tolerance are found with all grids of an evaluation set in
-one batched launch per chunk of sweeps and a residual check between chunks.
+Every solve is timed with CUDA events around all of its GPU work: the
+network's inference, the fallback check, every sweep and every residual
+check (one every 500 sweeps for the plain loop; one per outer step of the
+refinement).  The plain loop this accelerates is the reference's sweep loop
+(src/stencil_cpu.cu:32-35, src/stencil_dispatch.cu:153-157).
 """
 from __future__ import annotations
 
@@ -27,25 +33,17 @@ import numpy as np
 
 from . import lib as _lib
 from . import stencil as S
+from . import unet as U
 from .unet import UNet
+
+CHECK_EVERY = 500        # sweeps between residual checks of the plain loop
+TRAIN_SIZE = 128         # grid side the network is trained (and applied) at
+IR_INNER = {"fp16": 500, "bf16": 100}  # correction sweeps per outer step
 
 
 def coons_fill(fields):
     """Border kept, interior = transfinite interpolation of the border."""
-    import torch
-    f = fields
-    n, h, w = f.shape
-    s = torch.linspace(0, 1, w, device=f.device)[None, None, :]
-    t = torch.linspace(0, 1, h, device=f.device)[None, :, None]
-    B, T = f[:, :1, :], f[:, -1:, :]
-    L, R = f[:, :, :1], f[:, :, -1:]
-    c00, c10 = f[:, :1, :1], f[:, :1, -1:]
-    c01, c11 = f[:, -1:, :1], f[:, -1:, -1:]
-    cp = ((1 - t) * B + t * T + (1 - s) * L + s * R -
-          ((1 - s) * (1 - t) * c00 + s * (1 - t) * c10 + (1 - s) * t * c01 + s * t * c11))
-    out = cp.clone()
-    out[:, 0, :], out[:, -1, :], out[:, :, 0], out[:, :, -1] = f[:, 0, :], f[:, -1, :], f[:, :, 0], f[:, :, -1]
-    return out.contiguous()
+    return U.coons_fill(fields.contiguous())
 
 
 def borders(seeds, size, device="cuda"):
@@ -112,118 +110,170 @@ def train(net, fields, sols, epochs=8, batch=64, lr=2e-3, log=None):
     return losses, time.time() - t0
 
 
-def predict(net, fields, mode="direct", train_size=128):
+def predict(net, fields, mode="coarse", train_size=TRAIN_SIZE):
     """Initial fields for `fields` (n, H, W).  mode 'direct' applies the fully
     convolutional network at H x W; 'coarse' applies it to the border sampled
-    at train_size x train_size and interpolates the prediction bilinearly."""
-    import torch
+    at train_size x train_size and interpolates the prediction bilinearly
+    (every step a kernel of this library)."""
     if mode == "direct":
         return net.predict(fields)
-    n, H, W = fields.shape
-    idx_y = torch.round(torch.linspace(0, H - 1, train_size, device=fields.device)).long()
-    idx_x = torch.round(torch.linspace(0, W - 1, train_size, device=fields.device)).long()
-    coarse = fields[:, idx_y][:, :, idx_x].contiguous()
-    # border of the coarse problem only (interior zero)
-    cf = torch.zeros_like(coarse)
-    cf[:, 0, :], cf[:, -1, :], cf[:, :, 0], cf[:, :, -1] = coarse[:, 0, :], coarse[:, -1, :], coarse[:, :, 0], coarse[:, :, -1]
-    pc = net.predict(cf.contiguous())
-    up = torch.nn.functional.interpolate(pc[:, None], size=(H, W), mode="bilinear",
-                                         align_corners=True)[:, 0]
-    out = up.clone()
-    out[:, 0, :], out[:, -1, :], out[:, :, 0], out[:, :, -1] = fields[:, 0, :], fields[:, -1, :], fields[:, :, 0], fields[:, :, -1]
-    return out.contiguous()
+    coarse = U.resample_border(fields, train_size, train_size)
+    pc = net.predict(coarse)
+    return U.upsample_bilinear(pc, fields)
 
 
 def residuals(grids):
     return [S.residual(g, 1) for g in grids]
 
 
-def sweeps_to_tol(inits, tol=1e-5, chunk=2000, max_sweeps=400000):
-    """Plain FP32 Jacobi from each initial field until the FP64 relative
-    residual is below tol; all unconverged grids advance together in one
-    batched launch per chunk.  Returns (sweeps per grid, device seconds)."""
-    import torch
-    n = len(inits)
-    cur = [u.clone() for u in inits]
-    other = [u.clone() for u in inits]
-    done = [0] * n
-    active = [k for k in range(n) if S.residual(cur[k], 1) >= tol]
-    elapsed = 0.0
-    while active:
-        step = chunk
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        res = run_batch([cur[k] for k in active], [other[k] for k in active], step)
-        e1.record()
-        e1.synchronize()
-        elapsed += e0.elapsed_time(e1) / 1e3
-        nxt = []
-        for k, r in zip(active, res):
-            if r.data_ptr() != cur[k].data_ptr():
-                cur[k], other[k] = r, cur[k]
-            done[k] += step
-            if S.residual(cur[k], 1) >= tol and done[k] < max_sweeps:
-                nxt.append(k)
-        active = nxt
-    return done, elapsed
+def solve_plain(u_init, tol=1e-5, check=CHECK_EVERY, max_sweeps=2_000_000):
+    """Plain FP32 Jacobi (the library's AUTO engine, bit-exact sweeps) from
+    u_init until the relative residual is below tol, checked every `check`
+    sweeps (stencil_solve: the loop runs in the library).  Returns (sweeps,
+    residual, result grid)."""
+    a, b = u_init.clone(), u_init.clone()
+    done, r, res = S.solve(a, b, 1, max_sweeps, tol, check)
+    return done, r, res
 
 
-def per_sweep_seconds(size=512, sweeps=2000):
-    """Time of one FP32 sweep of one size x size grid on the plain kernel
-    (cluster engine, shared-memory resident)."""
+def solve_ir(u_init, storage, tol=1e-5, inner=None, workspace=None, max_sweeps=2_000_000):
+    """Mixed-precision refinement from u_init to tol (residual checked after
+    every outer step).  Returns (sweeps, residual, result grid)."""
+    u = u_init.clone()
+    r = S.ir_solve_ex(u, 1, max_sweeps, storage, inner_sweeps=inner or IR_INNER[storage], tol=tol,
+                      check_every=1, workspace=workspace)
+    return r["sweeps"], r["rel_residual"], u
+
+
+def timed(fn):
+    """(fn's result, seconds) with CUDA events on the current stream around it."""
     import torch
-    u = S.init_laplace2d((size, size), 5)
-    a, b = u.clone(), u.clone()
-    S.sweep(a, b, 1, 200, _lib.MODE_JACOBI, "auto")
-    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    S.sweep(a, b, 1, sweeps, _lib.MODE_JACOBI, "auto")
+    out = fn()
     e1.record()
     e1.synchronize()
-    return e0.elapsed_time(e1) / 1e3 / sweeps
+    return out, e0.elapsed_time(e1) / 1e3
 
 
-def evaluate(net, seeds, size=512, tol=1e-5, chunk=2000, log=print):
-    """Sweeps and time to tol for each arm on the held-out seeds."""
+def warm_init(net, field, mode="coarse", train_size=TRAIN_SIZE):
+    """The learned initial field of one problem (1, H, W) with the fallback
+    rule: the prediction only where its relative residual is below that of
+    the zero interior, which is 1 (its residual is the border term b itself)."""
+    pred = predict(net, field, mode, train_size)[0]
+    used = S.residual(pred, 1) < 1.0
+    return (pred if used else field[0]), used
+
+
+ARMS = {
+    # name: (initial field, solver)
+    "zero_fp32": ("zero", "fp32"),
+    "zero_ir_fp16": ("zero", "fp16"),
+    "learned_fp32": ("learned", "fp32"),
+    "learned_ir_fp16": ("learned", "fp16"),
+    "learned_ir_bf16": ("learned", "bf16"),
+    "coons_fp32": ("coons", "fp32"),
+    "direct_fp32": ("direct", "fp32"),
+}
+
+
+def solve_arm(net, field, arm, tol, ws, train_size=TRAIN_SIZE, check=CHECK_EVERY):
+    """One timed solve of problem `field` (1, H, W): returns (sweeps,
+    residual, seconds, prediction used, result).  `check`: sweeps between
+    the plain loop's residual checks."""
+    init, solver = ARMS[arm]
+
+    def run():
+        used = False
+        if init == "zero":
+            u0 = field[0]
+        elif init == "coons":
+            u0, used = coons_fill(field)[0], True
+        else:
+            u0, used = warm_init(net, field, "coarse" if init == "learned" else "direct",
+                                 train_size)
+        if solver == "fp32":
+            sw, r, u = solve_plain(u0, tol, check)
+        else:
+            sw, r, u = solve_ir(u0, solver, tol, workspace=ws[solver])
+        return sw, r, used, u
+
+    (sw, r, used, u), sec = timed(run)
+    return sw, r, sec, used, u
+
+
+def exact_steady_state(field):
+    """The FP64 steady state of one problem (H, W numpy array, border on the
+    outer ring), the accuracy check of the solves (not part of them): the
+    5-point Laplace system (4 u - sum of the 4 neighbours = border terms) is
+    diagonalised by the type-I discrete sine transform in each axis, with
+    eigenvalues 4 - 2 cos(p pi/(w+1)) - 2 cos(q pi/(h+1)), so one forward
+    transform, a division and one inverse transform solve it to FP64
+    rounding."""
+    from scipy import fft
+    f = np.asarray(field, np.float64)
+    H, W = f.shape
+    h, w = H - 2, W - 2
+    b = np.zeros((h, w))
+    b[0, :] += f[0, 1:-1]
+    b[-1, :] += f[-1, 1:-1]
+    b[:, 0] += f[1:-1, 0]
+    b[:, -1] += f[1:-1, -1]
+    lam = (4.0 - 2.0 * np.cos(np.pi * np.arange(1, h + 1) / (h + 1))[:, None]
+           - 2.0 * np.cos(np.pi * np.arange(1, w + 1) / (w + 1))[None, :])
+    out = f.copy()
+    out[1:-1, 1:-1] = fft.idstn(fft.dstn(b, type=1) / lam, type=1)
+    return out
+
+
+def evaluate(net, seeds, size=512, tol=1e-5, arms=None, n_exact=4, log=print):
+    """Iterations, time and accuracy to tol of every arm on the held-out
+    seeds, one problem at a time on the whole GPU."""
     import torch
-    f = borders(seeds, size)
-    arms = {}
-    t_sweep = per_sweep_seconds(size)
-    # plain: zero interior
-    arms["zero"] = f.clone()
-    arms["coons"] = coons_fill(f)
+    arms = list(arms or ["zero_fp32", "learned_fp32", "learned_ir_fp16", "learned_ir_bf16",
+                         "zero_ir_fp16"])
+    fields = borders(seeds, size)
+    ws = {st: S.ir_workspace((size, size), 1, st) for st in ("fp16", "bf16")}
+    # warm-up: kernels loaded, network buffers and engine plans made (untimed)
+    for arm in arms:
+        solve_arm(net, fields[:1], arm, 1e-2, ws)
     torch.cuda.synchronize()
-    t0 = time.time()
-    for mode in ("direct", "coarse"):
-        predict(net, f, mode)  # warm-up: allocates the activation buffers for this shape
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        p = predict(net, f, mode)
-        e1.record()
-        e1.synchronize()
-        arms["net_" + mode] = p
-        arms["net_" + mode + "_infer_s"] = e0.elapsed_time(e1) / 1e3 / len(seeds)
-    out = {"per_sweep_s": t_sweep, "size": size, "tol": tol, "n": len(seeds)}
-    r_zero = residuals(list(arms["zero"]))
-    for name in ("zero", "coons", "net_direct", "net_coarse"):
-        inits = list(arms[name])
-        r0 = residuals(inits)
-        # fallback rule: keep the prediction only where its residual is lower than zero init's
-        chosen = [inits[k] if r0[k] < r_zero[k] else arms["zero"][k] for k in range(len(inits))]
-        used = sum(1 for k in range(len(inits)) if r0[k] < r_zero[k])
-        sw, dev_s = sweeps_to_tol(chosen, tol, chunk)
-        infer = arms.get(name + "_infer_s", 0.0)
-        out[name] = {"mean_sweeps": float(np.mean(sw)), "median_sweeps": float(np.median(sw)),
-                     "initial_residual_median": float(np.median(r0)), "prediction_used": used,
-                     "time_per_solve_s": float(np.mean(sw)) * t_sweep + infer,
-                     "infer_s_per_grid": infer}
-        log("%-11s sweeps mean %.0f  r0 median %.3e  used %d/%d  time/solve %.4f s"
-            % (name, out[name]["mean_sweeps"], out[name]["initial_residual_median"], used,
-               len(inits), out[name]["time_per_solve_s"]))
-    for name in ("coons", "net_direct", "net_coarse"):
-        out[name]["speedup_vs_zero"] = out["zero"]["time_per_solve_s"] / out[name]["time_per_solve_s"]
+    exact = {}
+    for k in range(min(n_exact, len(seeds))):
+        try:
+            exact[k] = exact_steady_state(fields[k].cpu().numpy())
+        except ImportError:
+            break
+    out = {"size": size, "tol": tol, "n": len(seeds), "check_every_plain": CHECK_EVERY,
+           "ir_inner_sweeps": dict(IR_INNER), "timing": "CUDA events around each solve "
+           "(inference, fallback check, sweeps, residual checks); one problem at a time"}
+    for arm in arms:
+        sweeps, secs, res, used, errs = [], [], [], 0, []
+        for k in range(len(seeds)):
+            sw, r, sec, u_used, u = solve_arm(net, fields[k:k + 1], arm, tol, ws)
+            sweeps.append(sw)
+            secs.append(sec)
+            res.append(r)
+            used += int(u_used)
+            if k in exact:
+                ex = exact[k]
+                errs.append(float(np.abs(u.cpu().numpy().astype(np.float64) - ex).max() /
+                                  np.abs(ex).max()))
+        out[arm] = {"mean_sweeps": float(np.mean(sweeps)), "median_sweeps": float(np.median(sweeps)),
+                    "time_per_solve_s": float(np.mean(secs)),
+                    "median_time_s": float(np.median(secs)),
+                    "max_rel_residual": float(np.max(res)), "prediction_used": used,
+                    "fp64_normwise_err_max": max(errs) if errs else None,
+                    "fp64_err_seeds": len(errs)}
+        log("%-16s sweeps mean %8.0f  time/solve %.4f s  max residual %.2e  used %d/%d  "
+            "err vs FP64 %s" % (arm, out[arm]["mean_sweeps"], out[arm]["time_per_solve_s"],
+                                out[arm]["max_rel_residual"], used, len(seeds),
+                                "%.2e" % max(errs) if errs else "-"))
+    base = out.get("zero_fp32")
+    if base:
+        for arm in arms:
+            if arm != "zero_fp32":
+                out[arm]["speedup_vs_plain"] = base["time_per_solve_s"] / out[arm]["time_per_solve_s"]
     return out
 
 
