@@ -19,6 +19,9 @@
  *                 border band equal in both buffers.
  *   TEMPORAL_T    sweeps fused per HBM round trip by the COOP variant
  *                 (0 = the library chooses).
+ * HEURISTIC keeps its name with two settings: true (1) leaves the block shape
+ * to this library (its per-kernel default or tuning table); 2 takes the
+ * reference's occupancy-based shape (stencil_heuristic_geometry).
  */
 #ifndef STENCIL_CONSTANTS_H
 #define STENCIL_CONSTANTS_H

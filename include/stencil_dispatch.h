@@ -344,6 +344,19 @@ STENCIL_API int stencil_release(void);
  * reference's shape pass this result as p->block_*. */
 STENCIL_API int stencil_heuristic_block(const stencil_params *p, int threads, int *bx, int *by,
                                         int *bz);
+/* The reference's HEURISTIC geometry (src/stencil_dispatch.cu:138-146): the
+ * thread count that cudaOccupancyMaxPotentialBlockSizeVariableSMem returns for
+ * the kernel this library runs in p->variant's role (BASE: the vector or
+ * scalar base kernel; SMEM, SMEM_PADDED, SMEM_REGISTER: the TMA tile kernel),
+ * with the dynamic shared memory of each candidate block given by the
+ * reference's set_smem (src/stencil_dispatch.cu:46-66) on the block that
+ * stencil_heuristic_block shapes from it (p->block_x = BLOCK_X, default 32;
+ * p->coarsen_x = COARSEN_X); then that shape.  With HEURISTIC == 2 the
+ * constants.h drop-in launches the one-sweep roles with this block (the 3-D
+ * SMEM_REGISTER role, whose stream kernel has fixed thread shapes, takes its
+ * x and y as the tile: 4 * bx by by cells). */
+STENCIL_API int stencil_heuristic_geometry(const stencil_params *p, int *threads, int *bx, int *by,
+                                           int *bz);
 
 STENCIL_API int stencil_version(int *abi_version, int *sm);
 
@@ -375,6 +388,15 @@ static inline int stencil_params_from_constants(stencil_params *p)
     else if (SMEM && PADDED) p->variant = STENCIL_VARIANT_SMEM_PADDED;
     else if (SMEM) p->variant = STENCIL_VARIANT_SMEM;
     else p->variant = STENCIL_VARIANT_BASE;
+    if (HEURISTIC == 2 && !COOP) {
+        /* the reference's occupancy-based block (src/stencil_dispatch.cu:143) */
+        int t = 0, bx = 0, by = 0, bz = 0;
+        p->block_x = BLOCK_X;
+        rc = stencil_heuristic_geometry(p, &t, &bx, &by, &bz);
+        if (rc) return rc;
+        p->block_x = bx; p->block_y = by;
+        p->block_z = (p->variant == STENCIL_VARIANT_SMEM_REGISTER && p->dims == 3) ? 0 : bz;
+    }
     return STENCIL_OK;
 }
 

@@ -100,6 +100,36 @@ class RefKernels:
             self.fns[variant] = (fn, smem)
         return self.fns[variant]
 
+    def heuristic_geometry(self, variant, heuristic_block):
+        """The reference's HEURISTIC geometry for this cubin's kernel
+        (src/stencil_dispatch.cu:138-146): cuOccupancyMaxPotentialBlockSize
+        -- the driver form of the runtime call the reference makes at :143 --
+        with calculate_smem (:103-112: set_smem of the block that
+        set_max_occupancy_block_dimensions, :89-101, shapes from the thread
+        count) as the shared-memory function; heuristic_block(threads) is that
+        shaping rule.  Returns (threads, bx, by, bz)."""
+        fn = ctypes.c_void_p()
+        name = kernel_name(variant, self.dims, self.cf).encode()
+        self._check(self.cu.cuModuleGetFunction(ctypes.byref(fn), self.mod, name), "cuModuleGetFunction")
+        # CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES = 8, as large as the device allows
+        self.cu.cuFuncSetAttribute(fn, 8, 200 * 1024)
+
+        def smem_of(threads):
+            bx, by, bz = heuristic_block(threads)
+            return smem_bytes(variant, self.dims, self.radius, bx, by, bz, self.cf)
+
+        CB = ctypes.CFUNCTYPE(ctypes.c_size_t, ctypes.c_int)
+        cb = CB(smem_of)
+        min_grid, block = ctypes.c_int(), ctypes.c_int()
+        self.cu.cuOccupancyMaxPotentialBlockSize.argtypes = [
+            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), ctypes.c_void_p, CB,
+            ctypes.c_size_t, ctypes.c_int]
+        self._check(self.cu.cuOccupancyMaxPotentialBlockSize(ctypes.byref(min_grid), ctypes.byref(block),
+                                                             fn, cb, 0, 0),
+                    "cuOccupancyMaxPotentialBlockSize")
+        t = block.value
+        return (t,) + tuple(heuristic_block(t))
+
     def grid(self):
         n = self.dim
         gx = (1 + (n - 1) // self.bx) // self.cf

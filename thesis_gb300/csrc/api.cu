@@ -23,6 +23,8 @@ bool tb3d_supported(const Geom &g);
 bool rows3d_supported(const Geom &g);
 int run_rows3d(const Geom &g, float *a, float *b, int iters, int shape, cudaStream_t s,
                float **res);
+const void *base_kernel_ptr(const Geom &g, int dims);
+const void *tile_kernel_ptr(int dims, int r);
 
 static thread_local char t_err[512];
 static thread_local long long t_launches = 0;
@@ -620,6 +622,58 @@ int stencil_heuristic_block(const stencil_params *p, int threads, int *bx, int *
     } else {
         *bx = p->block_x, *by = threads / p->block_x, *bz = 1;
     }
+    return STENCIL_OK;
+}
+
+// The reference's set_smem (src/stencil_dispatch.cu:46-66): dynamic shared
+// memory of a block of the role's kernel, COARSEN_X cells per thread in x.
+static long long ref_role_smem(const stencil_params &p, int bx, int by, int bz) {
+    if (p.variant == STENCIL_VARIANT_BASE) return 0;
+    const long long R = p.radius, cf = std::max(p.coarsen_x, 1);
+    const long long sx = (long long)bx * cf, px = sx + 2 * R, py = by + 2 * R, pz = bz + 2 * R;
+    if (p.dims == 3) {
+        if (p.variant == STENCIL_VARIANT_SMEM_PADDED) return px * py * pz * 4;
+        if (p.variant == STENCIL_VARIANT_SMEM_REGISTER) return px * py * bz * 4;
+        return sx * by * bz * 4;
+    }
+    if (p.variant == STENCIL_VARIANT_SMEM_PADDED) return px * py * 4;
+    if (p.variant == STENCIL_VARIANT_SMEM_REGISTER) return px * by * 4;
+    return sx * by * 4;
+}
+
+// calculate_smem (src/stencil_dispatch.cu:103-112): threads -> the shaped
+// block's shared memory.
+struct RefRoleSmem {
+    stencil_params p;
+    size_t operator()(int threads) const {
+        int bx = 0, by = 0, bz = 0;
+        if (stencil_heuristic_block(&p, threads, &bx, &by, &bz)) return 0;
+        return (size_t)ref_role_smem(p, bx, by, bz);
+    }
+};
+
+int stencil_heuristic_geometry(const stencil_params *p, int *threads, int *bx, int *by, int *bz) {
+    int rc = stencil_params_check(p);
+    if (rc) return rc;
+    if (!threads || !bx || !by || !bz) return fail(STENCIL_EINVAL, "null argument");
+    stencil_params q = *p;
+    if (q.block_x < 1) q.block_x = 32;  // BLOCK_X's default (include/constants.h)
+    if (q.variant == STENCIL_VARIANT_AUTO || q.variant == STENCIL_VARIANT_COOP ||
+        q.variant == STENCIL_VARIANT_CLUSTER)
+        return fail(STENCIL_EINVAL, "the heuristic shapes the one-sweep roles (BASE, SMEM, "
+                                    "SMEM_PADDED, SMEM_REGISTER)");
+    const Geom g = make_geom(q);
+    const void *fn = q.variant == STENCIL_VARIANT_BASE ? base_kernel_ptr(g, q.dims)
+                                                       : tile_kernel_ptr(q.dims, q.radius);
+    if (!fn) return fail(STENCIL_EUNSUPPORTED, "no kernel for this role at radius %d", q.radius);
+    // cudaOccupancyMaxPotentialBlockSizeVariableSMem, as the reference calls it
+    // (src/stencil_dispatch.cu:143), on the kernel this library runs for the role
+    int min_grid = 0, t = 0;
+    RefRoleSmem smem{q};
+    ST_CUDA(cudaOccupancyMaxPotentialBlockSizeVariableSMem(&min_grid, &t, fn, smem));
+    rc = stencil_heuristic_block(&q, t, bx, by, bz);
+    if (rc) return rc;
+    *threads = t;
     return STENCIL_OK;
 }
 

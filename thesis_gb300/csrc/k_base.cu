@@ -122,6 +122,14 @@ bool grid_ok(dim3 grid) { return grid.y <= 65535u && grid.z <= 65535u && grid.x 
 
 }  // namespace
 
+// The kernel launch_base_sweep runs for this grid on 16-byte aligned buffers.
+const void *base_kernel_ptr(const Geom &g, int dims) {
+    VecFn fn = g.nx % 4 == 0 ? (dims == 3 ? vec_kernel<3>(g.radius) : vec_kernel<2>(g.radius)) : nullptr;
+    if (fn) return reinterpret_cast<const void *>(fn);
+    return dims == 3 ? reinterpret_cast<const void *>(k_base_any<3>)
+                     : reinterpret_cast<const void *>(k_base_any<2>);
+}
+
 int launch_base_sweep(const Geom &g, int dims, const float *src, float *dst, int bx, int by,
                       int bz, int cf, cudaStream_t s) {
     if (bx <= 0) bx = 32;

@@ -80,7 +80,10 @@ __device__ __forceinline__ float2 div_pair(float2 a) {
 // MULTI: one cooperative launch runs `sweeps` sweeps, ping-ponging between
 // (map0 -> dst0) and (map1 -> dst1), with a grid-wide barrier on *grid_bar
 // between sweeps; otherwise one sweep map0 -> dst0.
-template <int R, int TX, int TY, int RY, int NS, bool MULTI>
+// XS: the x-neighbour chunks come from the neighbouring lanes' centre chunks
+// by warp shuffles (only the lanes at the tile's x edges read the halo chunk
+// from shared memory) instead of two 16-byte shared loads per row.
+template <int R, int TX, int TY, int RY, int NS, bool MULTI, bool XS = false>
 __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, StreamShape<R, TX, TY, RY, NS>::MIN_BLOCKS)
     k_stream3d(const __grid_constant__ CUtensorMap map0, const __grid_constant__ CUtensorMap map1,
                float *dst0, float *dst1, Geom g, int tiles_x, int tiles_y, int zchunk, int items,
@@ -210,13 +213,31 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, Strea
 #pragma unroll
                 for (int r = 0; r < RY; ++r) {
                     float w[4 + 2 * S::RA];
+                    if constexpr (XS) {
+                        static_assert(S::RA == 4 && (S::CW == 16 || S::CW == 32), "shuffle form: R <= 4, 16 or 32 lanes per row");
+                        const float4 cc = col[r + R];
+                        float4 a, b;
+                        a.x = __shfl_up_sync(0xffffffffu, cc.x, 1, S::CW);
+                        a.y = __shfl_up_sync(0xffffffffu, cc.y, 1, S::CW);
+                        a.z = __shfl_up_sync(0xffffffffu, cc.z, 1, S::CW);
+                        a.w = __shfl_up_sync(0xffffffffu, cc.w, 1, S::CW);
+                        b.x = __shfl_down_sync(0xffffffffu, cc.x, 1, S::CW);
+                        b.y = __shfl_down_sync(0xffffffffu, cc.y, 1, S::CW);
+                        b.z = __shfl_down_sync(0xffffffffu, cc.z, 1, S::CW);
+                        b.w = __shfl_down_sync(0xffffffffu, cc.w, 1, S::CW);
+                        if (cx == 0) a = lds4(cb + r * S::PW - 4);
+                        if (cx == S::CW - 1) b = lds4(cb + r * S::PW + 4);
+                        w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w;
+                        w[8] = b.x; w[9] = b.y; w[10] = b.z; w[11] = b.w;
+                    } else {
 #pragma unroll
-                    for (int h = 0; h < S::RA / 4; ++h) {
-                        const float4 a = lds4(cb + r * S::PW - S::RA + 4 * h);
-                        const float4 b = lds4(cb + r * S::PW + 4 + 4 * h);
-                        w[4 * h] = a.x; w[4 * h + 1] = a.y; w[4 * h + 2] = a.z; w[4 * h + 3] = a.w;
-                        w[S::RA + 4 + 4 * h] = b.x; w[S::RA + 5 + 4 * h] = b.y;
-                        w[S::RA + 6 + 4 * h] = b.z; w[S::RA + 7 + 4 * h] = b.w;
+                        for (int h = 0; h < S::RA / 4; ++h) {
+                            const float4 a = lds4(cb + r * S::PW - S::RA + 4 * h);
+                            const float4 b = lds4(cb + r * S::PW + 4 + 4 * h);
+                            w[4 * h] = a.x; w[4 * h + 1] = a.y; w[4 * h + 2] = a.z; w[4 * h + 3] = a.w;
+                            w[S::RA + 4 + 4 * h] = b.x; w[S::RA + 5 + 4 * h] = b.y;
+                            w[S::RA + 6 + 4 * h] = b.z; w[S::RA + 7 + 4 * h] = b.w;
+                        }
                     }
                     const float4 c = col[r + R];
                     w[S::RA] = c.x; w[S::RA + 1] = c.y; w[S::RA + 2] = c.z; w[S::RA + 3] = c.w;
@@ -359,12 +380,12 @@ struct StreamKernel {
     int tx, ty, threads, smem;
 };
 
-template <int R, int TX, int TY, int RY, int NS, bool WITH_MULTI = false>
+template <int R, int TX, int TY, int RY, int NS, bool WITH_MULTI = false, bool XS = false>
 StreamKernel sk() {
     using S = StreamShape<R, TX, TY, RY, NS>;
     const void *multi = nullptr;
-    if constexpr (WITH_MULTI) multi = reinterpret_cast<const void *>(k_stream3d<R, TX, TY, RY, NS, true>);
-    return {reinterpret_cast<const void *>(k_stream3d<R, TX, TY, RY, NS, false>), multi, TX, TY,
+    if constexpr (WITH_MULTI) multi = reinterpret_cast<const void *>(k_stream3d<R, TX, TY, RY, NS, true, XS>);
+    return {reinterpret_cast<const void *>(k_stream3d<R, TX, TY, RY, NS, false, XS>), multi, TX, TY,
             S::THREADS, S::SMEM_BYTES};
 }
 
@@ -375,6 +396,17 @@ StreamKernel sk() {
 // thread (half the y-halo rows per output row).  The persistent form exists
 // for the shape it uses (R = 1: 3, R = 2: 5, R >= 3: 4).
 StreamKernel pick(int r, int shape) {
+    // shape 6: the persistent-form shape of the radius with x neighbours by
+    // warp shuffles (A/B against the shared-memory reads)
+    if (shape == 6) {
+        switch (r) {
+            case 1: return sk<1, 128, 16, 1, 16, false, true>();
+            case 2: return sk<2, 128, 32, 2, 8, false, true>();
+            case 3: return sk<3, 128, 16, 1, 8, false, true>();
+            case 4: return sk<4, 128, 16, 1, 8, false, true>();
+            default: return {nullptr, nullptr, 0, 0, 0, 0};
+        }
+    }
     switch (r) {
         case 1: return shape == 5 ? sk<1, 128, 32, 2, 8>() : shape == 3 ? sk<1, 128, 16, 1, 16, true>() : shape == 2 ? sk<1, 128, 16, 1, 8>() : shape == 1 ? sk<1, 64, 32, 2, 8>() : sk<1, 128, 16, 2, 8>();
         case 2: return shape == 5 ? sk<2, 128, 32, 2, 8, true>() : shape == 3 ? sk<2, 128, 16, 1, 16>() : shape == 2 ? sk<2, 128, 16, 1, 8>() : shape == 1 ? sk<2, 64, 32, 2, 8>() : sk<2, 128, 16, 2, 8>();
@@ -442,8 +474,8 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     // either way).
     int shape = (!tile_x && !tile_y) ? (R <= 2 ? 3 : 4)
                                      : (tile_y == 1 ? 2 : ((tile_x && tile_x < 128) || tile_y > 16 ? 1 : 0));
-    if (shape_hint >= 1 && shape_hint <= 5) shape = shape_hint;
-    if (persistent && !(shape_hint >= 1 && shape_hint <= 5)) shape = R == 1 ? 3 : (R == 2 ? 5 : 4);
+    if (shape_hint >= 1 && shape_hint <= 6) shape = shape_hint;
+    if (persistent && !(shape_hint >= 1 && shape_hint <= 6)) shape = R == 1 ? 3 : (R == 2 ? 5 : 4);
     StreamKernel k = pick(R, shape);
     if (!k.fn) return fail(STENCIL_EUNSUPPORTED, "stream kernel has no radius-%d instance", R);
     if (persistent && !k.multi)

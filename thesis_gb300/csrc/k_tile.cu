@@ -98,6 +98,18 @@ const void *tile_kernel(int r) {
 
 }  // namespace
 
+// The kernel launch_tile_sweep runs (null if none), with its dynamic
+// shared-memory limit raised to the largest box the launcher allows.
+const void *tile_kernel_ptr(int dims, int r) {
+    const void *fn = dims == 3 ? tile_kernel<3>(r) : tile_kernel<2>(r);
+    if (fn && cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024 + 256) !=
+                  cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return fn;
+}
+
 bool tile_supported(const Geom &g, int dims) {
     (void)dims;
     return g.nx % 4 == 0 && (g.radius <= 4 || g.radius == 8);

@@ -99,6 +99,8 @@ def load() -> ctypes.CDLL:
         "stencil_last_dispatch": (i, [ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_longlong)]),
         "stencil_heuristic_block": (i, [P, i, ctypes.POINTER(i), ctypes.POINTER(i),
                                         ctypes.POINTER(i)]),
+        "stencil_heuristic_geometry": (i, [P, ctypes.POINTER(i), ctypes.POINTER(i),
+                                           ctypes.POINTER(i), ctypes.POINTER(i)]),
         "stencil_run_host_timed": (i, [P, vp, vp, ctypes.POINTER(ctypes.c_float),
                                        ctypes.POINTER(ctypes.c_float)]),
         "stencil_init_reference": (i, [P, vp, vp]),

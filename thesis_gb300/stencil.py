@@ -53,9 +53,31 @@ class StencilConfig:
         return _lib.VARIANT_BASE
 
     def params(self) -> _lib.StencilParams:
+        """HEURISTIC: False = the BLOCK_* shape; True (1) = the library's
+        choice; 2 = the reference's occupancy-based shape
+        (stencil_heuristic_geometry)."""
         block = (0, 0, 0) if self.HEURISTIC else (self.BLOCK_X, self.BLOCK_Y, self.BLOCK_Z)
-        return _lib.make_params(self.shape, self.RADIUS, self.ITERATIONS, self.STENCIL_MODE,
-                                self.variant(), block, self.COARSEN_X, self.TEMPORAL_T)
+        p = _lib.make_params(self.shape, self.RADIUS, self.ITERATIONS, self.STENCIL_MODE,
+                             self.variant(), block, self.COARSEN_X, self.TEMPORAL_T)
+        if self.HEURISTIC == 2 and not self.COOP:
+            p.block_x = self.BLOCK_X
+            t, bx, by, bz = heuristic_geometry(p)
+            # the 3-D stream kernel (SMEM_REGISTER) takes x and y as its tile
+            if p.variant == _lib.VARIANT_SMEM_REGISTER and p.dims == 3:
+                bz = 0
+            p.block_x, p.block_y, p.block_z = bx, by, bz
+        return p
+
+
+def heuristic_geometry(params: _lib.StencilParams):
+    """(threads, bx, by, bz) of the reference's HEURISTIC selection for these
+    parameters (stencil_heuristic_geometry)."""
+    t, bx, by, bz = (ctypes.c_int() for _ in range(4))
+    _lib.check(_lib.load().stencil_heuristic_geometry(ctypes.byref(params), ctypes.byref(t),
+                                                      ctypes.byref(bx), ctypes.byref(by),
+                                                      ctypes.byref(bz)),
+               "stencil_heuristic_geometry")
+    return t.value, bx.value, by.value, bz.value
 
 
 def _stream_handle(stream):
