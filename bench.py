@@ -480,8 +480,17 @@ def bench_c4(S, lib, torch):
                 for k in range(0, len(specs), 8)]
 
     csize, _ = A.tune_batch_cluster_size(sample_jobs, log=None)
+
+    def class_jobs(cls):
+        # up to 6 grids of the class with a tenth of their sweeps: the proxy
+        # the tuner times (fresh copies, so the benchmark grids stay as made)
+        ks = [k for k, sp in enumerate(specs) if A.batch_class(sp[0]) == cls][:6]
+        return [(grids[k][0].clone(), grids[k][1].clone(), specs[k][1],
+                 max(10, specs[k][2] // 10), lib.MODE_JACOBI) for k in ks]
+
+    tuned = A.tune_batch(class_jobs, log=None)
     jobs = [(g[0], g[1], sp[1], sp[2], lib.MODE_JACOBI) for g, sp in zip(grids, specs)]
-    bt = S.Batch(jobs, cluster_size=csize)
+    bt = S.Batch(jobs, cluster_size=csize, hints_for=A.batch_hints({"batch": tuned}))
     stream = torch.cuda.Stream()
     graph = torch.cuda.CUDAGraph()
     with torch.cuda.stream(stream):
@@ -509,6 +518,7 @@ def bench_c4(S, lib, torch):
             "s_per_batch": round(min(times), 3), "cell_updates": ups, "cluster_size": csize,
             "device_bytes": mem, "graph_replays_per_batch": 1, "kernel_launches_per_batch": launches,
             "cluster_jobs": cluster_jobs, "whole_gpu_jobs": whole_gpu_jobs, "graph": True,
+            "tuned": {c: r["choice"] for c, r in tuned.items()},
             "roofline_frac_if_hbm": round(ups / min(times) * 8 / 1e9 / peaks()[0], 4)}
 
 

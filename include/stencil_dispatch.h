@@ -65,8 +65,10 @@ enum {
     STENCIL_VARIANT_SMEM_PADDED = 3,   /* same kernel as SMEM */
     STENCIL_VARIANT_SMEM_REGISTER = 4, /* 2.5D stream along the slowest axis */
     STENCIL_VARIANT_COOP = 5,          /* all sweeps in one cooperative launch; 3-D: one
-                                          sweep per HBM pass (temporal 0 or 1) or
-                                          `temporal` (>= 2, JACOBI, R <= 2) per pass;
+                                          sweep per HBM pass (temporal 0 or 1; block_z
+                                          1..6 = a stream-kernel shape with a
+                                          persistent form) or `temporal` (>= 2, JACOBI,
+                                          R <= 2) per pass;
                                           2-D grids of at most one tile per SM: every SM,
                                           `temporal` sweeps per halo exchange, tile
                                           block_x * coarsen_x by block_y cells (0: chosen);
@@ -164,7 +166,16 @@ typedef struct stencil_batch_job {
     float *d_u1, *d_u2;
     int dims, nx, ny, nz;
     int radius, iterations, mode;
-    int reserved; /* must be zero */
+    /* Tuning hints (0 = the library's choice), as an autotuner sets them:
+     * temporal: sweeps between halo exchanges -- for a job kept in a
+     * cluster's shared memory the most it may use (the largest of 8, 4, 2, 1
+     * at most this that fits), for a 2-D job with a whole-GPU launch the
+     * temporally blocked engine's depth, and for a 3-D one with a whole-GPU
+     * launch >= 2 selects the temporally blocked kernel with that depth (R
+     * <= 2, JACOBI; else the one-sweep-per-pass stream kernel);
+     * tile_x, tile_y: the 2-D whole-GPU engine's tile in cells. */
+    int temporal, tile_x, tile_y;
+    int reserved[3]; /* must be zero */
 } stencil_batch_job;
 
 /* Device workspace bytes for njobs jobs (a job table and the queue counter). */

@@ -77,3 +77,17 @@ def test_tune_on_gpu_and_auto_uses_it(cuda):
     want = S.sweep(u.clone(), u.clone(), 1, 7, L.MODE_JACOBI, "base").cpu().numpy()
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     L.load().stencil_tuning_clear()
+
+
+def test_search_space_covers_3d_temporal_blocking_and_batch_classes():
+    top, sub = A.variant_space((256, 256, 256), 1)
+    assert {"variant": "coop"} in top and sub["coop"]["temporal"] == [0, 2, 3, 4]
+    _, sub4 = A.variant_space((256, 256, 256), 4)
+    assert sub4["coop"]["temporal"] == [0]  # temporal blocking needs R <= 2
+    assert A.batch_class((128, 128)) == "2d_small" and A.batch_class((2048, 2048)) == "2d_large"
+    assert A.batch_class((96, 96, 96)) == "3d_small" and A.batch_class((200, 200, 200)) == "3d_large"
+    assert set(A.BATCH_SPACE) == {"2d_small", "2d_large", "3d_small", "3d_large"}
+    db = {"batch": {"3d_large": {"choice": {"temporal": 2, "tile": [0, 0]}}}}
+    hints = A.batch_hints(db)
+    assert hints((200, 200, 200)) == {"temporal": 2, "tile": [0, 0]}
+    assert hints((64, 64)) is None and A.batch_hints({})((64, 64)) is None

@@ -96,6 +96,18 @@ def test_pool_upsample_relu_add_head(cuda):
     assert (out.cpu().double() - ref).abs().max().item() < 1e-4
 
 
+# Normwise relative error of each gradient against torch float64 on the same
+# BF16 inputs: twice the error measured on a GB300 for this seed (the BF16
+# rounding of the activations between layers dominates it; the weight
+# gradients sum in FP32 with atomics, so repeated runs differ in the last
+# bits only).
+GRAD_BOUND = {
+    "e0a": 0.025, "e0b": 0.033, "e1a": 0.083, "e1b": 0.058, "e2a": 0.105, "e2b": 0.079,
+    "ba": 0.125, "bb": 0.098, "d2a": 0.056, "d2b": 0.038, "d1a": 0.021, "d1b": 0.017,
+    "d0a": 0.005, "d0b": 0.0061, "head": 0.05,
+}
+
+
 def test_network_gradients_match_cpu_reference(cuda):
     """Loss and every parameter gradient of the BF16 network vs torch float64."""
     import torch
@@ -126,7 +138,7 @@ def test_network_gradients_match_cpu_reference(cuda):
     # the library accumulates the sum of squares; the reference returns the mean
     loss_rel = abs(loss_gpu / (n * (h - 2) * (w - 2)) - loss.item()) / abs(loss.item())
     print("loss relative error %.3e" % loss_rel)
-    assert loss_gpu / (n * (h - 2) * (w - 2)) == pytest.approx(loss.item(), rel=5e-2)
+    assert loss_gpu / (n * (h - 2) * (w - 2)) == pytest.approx(loss.item(), rel=1e-5)
     worst = 0.0
     for name, _, _ in R.LAYERS:
         for k, ref in (("dw", params[name][0].grad), ("db", params[name][1].grad)):
@@ -136,8 +148,10 @@ def test_network_gradients_match_cpu_reference(cuda):
             rel = (got - ref).norm().item() / max(ref.norm().item(), 1e-30)
             worst = max(worst, rel)
             print("gradient %s.%s normwise error %.3e" % (name, k, rel))
-            assert rel < 0.1, (name, k, rel)
+            assert rel < GRAD_BOUND[name], (name, k, rel)
     print("worst normwise gradient error %.3e" % worst)
     for k, ref in (("dw", hw.grad), ("db", hb.grad)):
         got = net.head[k].cpu().double()
-        assert (got - ref).norm().item() / max(ref.norm().item(), 1e-30) < 0.1
+        rel = (got - ref).norm().item() / max(ref.norm().item(), 1e-30)
+        print("gradient head.%s normwise error %.3e" % (k, rel))
+        assert rel < GRAD_BOUND["head"], (k, rel)

@@ -20,7 +20,11 @@ Here every candidate runs in-process through the C ABI:
     Autotuning/tuner/evaluator.py);
   * results go to a JSON database (dims, radius, size bucket) -> choice,
     which load_db() installs into the library (stencil_tuning_set) so that
-    STENCIL_VARIANT_AUTO uses it.
+    STENCIL_VARIANT_AUTO uses it;
+  * batches (tune_batch): per class of grid (2-D / 3-D, on a cluster or with
+    a whole-GPU launch) the sweeps between halo exchanges, the 3-D temporal
+    blocking depth and the 2-D tile, stored in the database's "batch" section
+    that Batch(hints_for=batch_hints(db)) applies.
 """
 from __future__ import annotations
 
@@ -76,6 +80,11 @@ def variant_space(shape, radius):
             sub["coop"] = {"temporal": [0, 2, 4, 6, 8, 10, 12, 16, 20],
                            "block": [(0, 0, 1), (16, 16, 1), (24, 20, 1), (32, 16, 1),
                                      (16, 32, 1), (32, 32, 1), (24, 24, 1)]}
+        if dims == 3 and radius <= 4:
+            # all sweeps in one cooperative launch: one sweep per HBM pass
+            # (temporal 0) or, at R <= 2, T sweeps per pass (temporal blocking)
+            top.append({"variant": "coop"})
+            sub["coop"] = {"temporal": [0, 2, 3, 4] if radius <= 2 else [0]}
     return top, sub
 
 
@@ -220,6 +229,101 @@ def tune_batch_cluster_size(make_jobs, sizes=(1, 2, 4, 8, 16), log=print):
         if t < best_t:
             best, best_t = c, t
     return best, best_t
+
+
+# ---- batches: per-class tuning fields of stencil_batch_job ------------------
+#
+# The batch engine runs a grid on a thread-block cluster when it fits the
+# cluster's shared memory (and, for 3-D, below about 106^3 from L2) and gives
+# larger ones a whole-GPU launch.  Each class has its own knobs:
+#   2d_small / 3d_small (on clusters): sweeps between halo exchanges in shared
+#     memory (temporal: a cap on 8, 4, 2, 1);
+#   2d_large (whole GPU): the temporally blocked engine's depth and tile where
+#     the grid fits one tile per SM;
+#   3d_large (whole GPU): temporal 0 = the one-sweep-per-pass stream kernel,
+#     >= 2 = the temporally blocked kernel with that depth (R <= 2).
+BATCH_SPACE = {
+    "2d_small": {"temporal": [0, 1, 2, 4, 8]},
+    "2d_large": {"temporal": [0, 2, 4, 8, 12, 16],
+                 "tile": [(0, 0), (32, 16), (64, 16), (32, 32), (64, 32), (128, 16)]},
+    "3d_small": {"temporal": [0, 1, 2, 4, 8]},
+    "3d_large": {"temporal": [0, 2, 3]},
+}
+
+
+def batch_class(shape) -> str:
+    side = max(shape)
+    if len(shape) == 2:
+        return "2d_small" if side <= 640 else "2d_large"
+    return "3d_small" if side <= 106 else "3d_large"
+
+
+def batch_hints(db):
+    """hints_for(shape) for thesis_gb300.stencil.Batch from a database's
+    "batch" section ({} when it has none)."""
+    table = (db or {}).get("batch", {})
+
+    def hints_for(shape):
+        return table.get(batch_class(shape), {}).get("choice")
+    return hints_for
+
+
+def tune_batch(make_jobs, classes=None, repeats=2, log=print):
+    """Per-class tuning of a batch: make_jobs(cls) returns fresh (d_u1, d_u2,
+    radius, iterations, mode) jobs of that class (a proxy of the batch, e.g.
+    some of its grids with fewer sweeps).  Each class's fields are chosen by
+    coordinate descent over BATCH_SPACE, scored by the CUDA-event time of one
+    batched launch (min over repeats); a candidate whose results differ from
+    the library's default choice in any bit is rejected.  Returns
+    {class: {"choice": {...}, "s": seconds, "default_s": ...}}."""
+    import torch
+    from . import stencil as S
+    out = {}
+    for cls in classes or list(BATCH_SPACE):
+        jobs = make_jobs(cls)
+        if not jobs:
+            continue
+        init = [(j[0].clone(), j[1].clone()) for j in jobs]
+        ref = None
+
+        def score(cfg):
+            nonlocal ref
+            hint = {"temporal": cfg.get("temporal", 0), "tile": tuple(cfg.get("tile", (0, 0)))}
+            best = float("inf")
+            for _ in range(repeats):
+                for (u1, u2), (a, b) in zip(init, jobs):
+                    a.copy_(u1)
+                    b.copy_(u2)
+                try:
+                    bt = S.Batch([tuple(j[:5]) + (hint,) for j in jobs])
+                except _lib.StencilError:
+                    return float("inf")
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                bt.launch()
+                e1.record()
+                e1.synchronize()
+                res = [bt.result(k).clone() for k in range(len(jobs))]
+                bt.close()
+                best = min(best, e0.elapsed_time(e1) / 1e3)
+            if ref is None:
+                ref = res
+            elif any(not torch.equal(x.view(torch.int32), y.view(torch.int32)) for x, y in zip(res, ref)):
+                return float("inf")
+            return best
+
+        start = {"temporal": 0, "tile": (0, 0)}
+        default_s = score(start)  # also records the reference results
+        space = {k: v for k, v in BATCH_SPACE[cls].items()}
+        best, best_s, n = coordinate_descent(start, space, score)
+        out[cls] = {"choice": {"temporal": best.get("temporal", 0), "tile": list(best.get("tile", (0, 0)))},
+                    "s": best_s, "default_s": default_s, "candidates": n, "jobs": len(jobs)}
+        if log:
+            log("batch %s: %s %.4f s (default %.4f s, %d candidates)"
+                % (cls, out[cls]["choice"], best_s, default_s, n))
+        del jobs, init, ref
+        torch.cuda.empty_cache()
+    return out
 
 
 def main():

@@ -357,9 +357,11 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
     }
     if (variant == STENCIL_VARIANT_COOP && p->dims == 3 && stream3d_supported(g)) {
         // One sweep per HBM pass, all sweeps in one persistent cooperative
-        // launch with a grid-wide barrier between them.
+        // launch with a grid-wide barrier between them (block_z 1..6 picks
+        // the stream kernel's shape where its persistent form exists).
         float *res = nullptr;
-        rc = run_stream3d(g, cur, nxt, p->iterations, 0, 0, s, &res, 0, true);
+        rc = run_stream3d(g, cur, nxt, p->iterations, 0, 0, s, &res,
+                          (p->block_z >= 1 && p->block_z <= 6) ? p->block_z : 0, true);
         if (rc) return rc;
         if (d_result) *d_result = res;
         return STENCIL_OK;

@@ -38,6 +38,8 @@
 
 namespace st {
 
+bool tb3d_supported(const Geom &g);
+
 struct ClusterJob {
     float *a, *b;       // caller buffers (a = initial state)
     int dims, nx, ny, nz;
@@ -487,16 +489,18 @@ bool cluster_job_ok(int dims, int nx, int ny, int nz, int radius) {
 
 // Resident when the slab fits and every CTA that owns slices owns at least R
 // (so each halo comes from one neighbour).
-// The sweeps between halo exchanges: the largest of 4, 2, 1 whose deeper
-// halo still fits and is owned by a single neighbour.
-static void plan_job(ClusterJob &j, int csize) {
+// The sweeps between halo exchanges: the largest of 4, 2, 1 (or of 8, 4,
+// 2, 1 at most tmax when a tuning hint gives one) whose deeper halo still
+// fits and is owned by a single neighbour.
+static void plan_job(ClusterJob &j, int csize, int tmax = 0) {
     const int S = j.dims == 3 ? j.nz : j.ny;
     const int H = (S + csize - 1) / csize;
     const int last = S - ((S + H - 1) / H - 1) * H;
     j.resident = 0;
     j.tblock = 1;
     j.pad = 0;
-    for (int tb : {4, 2, 1}) {
+    for (int tb : {8, 4, 2, 1}) {
+        if (tmax > 0 ? tb > tmax : tb > 4) continue;
         const int ht = tb * j.radius;
         if (slab_bytes(j, csize, tb) + 128 <= kClusterSmemMax && H >= ht && last >= ht) {
             j.resident = 1;
@@ -589,7 +593,8 @@ int max_active_clusters(int csize) {
     return std::max(1, v);
 }
 
-ClusterJob make_job(const Geom &g, int dims, float *a, float *b, int iters, int csize) {
+ClusterJob make_job(const Geom &g, int dims, float *a, float *b, int iters, int csize,
+                    int tmax = 0) {
     ClusterJob j;
     j.a = a;
     j.b = b;
@@ -600,7 +605,7 @@ ClusterJob make_job(const Geom &g, int dims, float *a, float *b, int iters, int 
     j.radius = g.radius;
     j.iters = iters;
     j.legacy = g.legacy;
-    plan_job(j, csize);
+    plan_job(j, csize, tmax);
     return j;
 }
 
@@ -670,6 +675,7 @@ struct StreamedJob {
     float *a, *b;
     int iters;
     int dims;
+    int temporal, tile_x, tile_y;  // tuning hints (0 = the library's choice)
 };
 
 struct BatchPlan {
@@ -752,14 +758,19 @@ extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, i
             return fail(STENCIL_EINVAL, "job %d: two distinct 16-byte aligned buffers required", i);
         if (!cluster_job_ok(b.dims, b.nx, b.ny, b.nz, b.radius))
             return fail(STENCIL_EUNSUPPORTED, "job %d: batch jobs need nx %% 4 == 0 and radius <= 4", i);
+        if (b.temporal < 0 || b.tile_x < 0 || b.tile_y < 0 || (b.tile_x % 4) || b.reserved[0] ||
+            b.reserved[1] || b.reserved[2])
+            return fail(STENCIL_EINVAL,
+                        "job %d: temporal, tile_x, tile_y >= 0, tile_x %% 4 == 0, reserved zero", i);
         const Geom g = make_geom(p);
-        ClusterJob j = make_job(g, p.dims, b.d_u1, b.d_u2, b.iterations, csize);
+        ClusterJob j = make_job(g, p.dims, b.d_u1, b.d_u2, b.iterations, csize, b.temporal);
         // small non-resident 3-D grids stay on clusters, many at a time: a
         // whole-GPU launch of one of them is latency-bound
         const bool big3d = (long long)cell_count(p) >= kStreamMinCells3d;
         if (!j.resident && ((p.dims == 3 && big3d && stream3d_supported(g)) ||
                             (p.dims == 2 && rows2d_supported(g, 2)))) {
-            plan.streamed.push_back({g, b.d_u1, b.d_u2, b.iterations, p.dims});
+            plan.streamed.push_back({g, b.d_u1, b.d_u2, b.iterations, p.dims, b.temporal, b.tile_x,
+                                     b.tile_y});
             continue;
         }
         table.push_back(j);
@@ -804,9 +815,15 @@ extern "C" int stencil_batch_launch(const void *d_workspace, stencil_stream_t st
         if (rc) return rc;
     }
     for (const StreamedJob &j : plan.streamed) {
-        int rc = j.dims == 3 ? run_stream3d(j.g, j.a, j.b, j.iters, 0, 0, s, nullptr, 0, true)
-                 : tb2d_supported(j.g, 2) ? run_tb2d(j.g, j.a, j.b, j.iters, 0, 0, 0, s, nullptr)
-                                          : run_rows2d(j.g, j.a, j.b, j.iters, s, nullptr);
+        int rc;
+        if (j.dims == 3)
+            rc = (j.temporal >= 2 && !j.g.legacy && tb3d_supported(j.g))
+                     ? run_tb3d(j.g, j.a, j.b, j.iters, j.temporal, s, nullptr)
+                     : run_stream3d(j.g, j.a, j.b, j.iters, 0, 0, s, nullptr, 0, true);
+        else
+            rc = tb2d_supported(j.g, 2)
+                     ? run_tb2d(j.g, j.a, j.b, j.iters, j.temporal, j.tile_x, j.tile_y, s, nullptr)
+                     : run_rows2d(j.g, j.a, j.b, j.iters, s, nullptr);
         if (rc) return rc;
     }
     return STENCIL_OK;

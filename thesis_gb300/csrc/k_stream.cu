@@ -401,7 +401,7 @@ StreamKernel pick(int r, int shape) {
     if (shape == 6) {
         switch (r) {
             case 1: return sk<1, 128, 16, 1, 16, false, true>();
-            case 2: return sk<2, 128, 32, 2, 8, false, true>();
+            case 2: return sk<2, 128, 32, 2, 8, true, true>();
             case 3: return sk<3, 128, 16, 1, 8, false, true>();
             case 4: return sk<4, 128, 16, 1, 8, false, true>();
             default: return {nullptr, nullptr, 0, 0, 0, 0};

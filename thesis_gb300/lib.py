@@ -39,7 +39,8 @@ class BatchJob(ctypes.Structure):
         ("d_u1", ctypes.c_void_p), ("d_u2", ctypes.c_void_p), ("dims", ctypes.c_int),
         ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
         ("radius", ctypes.c_int), ("iterations", ctypes.c_int), ("mode", ctypes.c_int),
-        ("reserved", ctypes.c_int),
+        ("temporal", ctypes.c_int), ("tile_x", ctypes.c_int), ("tile_y", ctypes.c_int),
+        ("reserved", ctypes.c_int * 3),
     ]
 
 

@@ -234,16 +234,25 @@ class Batch:
     """Many grids of uneven sizes and sweep counts in one persistent launch
     (stencil_batch_prepare / stencil_batch_launch).
 
-    jobs: list of (d_u1, d_u2, radius, iterations, mode) with CUDA float32
-    tensors of shape (ny, nx) or (nz, ny, nx).  After ``launch`` each job's
-    result is in d_u1 for an even sweep count, else in d_u2 (``result(i)``).
+    jobs: list of (d_u1, d_u2, radius, iterations, mode[, hints]) with CUDA
+    float32 tensors of shape (ny, nx) or (nz, ny, nx); hints (optional dict)
+    sets the job's tuning fields "temporal" and "tile" (tile_x, tile_y).
+    hints_for(shape) -> dict, when given, supplies hints for jobs without
+    their own (e.g. autotune.batch_hints of a tuning database).  After
+    ``launch`` each job's result is in d_u1 for an even sweep count, else in
+    d_u2 (``result(i)``).
     """
 
-    def __init__(self, jobs, cluster_size: int = 0, stream=None):
+    def __init__(self, jobs, cluster_size: int = 0, stream=None, hints_for=None):
         import torch
-        self.jobs = list(jobs)
+        self.jobs = [tuple(j[:5]) for j in jobs]
+        hints = [j[5] if len(j) > 5 else None for j in jobs]
         arr = (_lib.BatchJob * max(1, len(self.jobs)))()
         for k, (u1, u2, radius, iters, mode) in enumerate(self.jobs):
+            h = hints[k] if hints[k] is not None else (hints_for(tuple(u1.shape)) if hints_for else None)
+            if h:
+                arr[k].temporal = int(h.get("temporal", 0))
+                arr[k].tile_x, arr[k].tile_y = (int(v) for v in h.get("tile", (0, 0)))
             _check_tensor(u1)
             _check_tensor(u2, u1.shape)
             j = arr[k]
