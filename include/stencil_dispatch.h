@@ -160,8 +160,11 @@ STENCIL_API int stencil_copy_border(const stencil_params *p, const float *d_src,
  * in ONE launch over a device work queue (no counterpart in the reference,
  * which runs one grid per process).  Each job is one grid with its own two
  * buffers; after the launch its result is in d_u1 for an even sweep count and
- * in d_u2 for an odd one, exactly as stencil_dispatch_ex would leave it.
- * Jobs need nx % 4 == 0 and radius <= 4. */
+ * in d_u2 for an odd one, as the ping-pong loop leaves it (the other buffer
+ * holds an earlier state).  Jobs need radius <= 4; a job whose nx is not a
+ * multiple of 4 (rows not 16-byte aligned) is swept in a copy with the row
+ * pitch rounded up to 4 cells, held in the workspace and copied in and out by
+ * stencil_batch_launch. */
 typedef struct stencil_batch_job {
     float *d_u1, *d_u2;
     int dims, nx, ny, nz;
@@ -178,8 +181,13 @@ typedef struct stencil_batch_job {
     int reserved[3]; /* must be zero */
 } stencil_batch_job;
 
-/* Device workspace bytes for njobs jobs (a job table and the queue counter). */
+/* Device workspace bytes for njobs jobs whose nx are multiples of 4 (a job
+ * table and the queue counter). */
 STENCIL_API int stencil_batch_workspace_bytes(int njobs, size_t *bytes);
+/* Device workspace bytes for these jobs: the job table and the pitched copies
+ * of the jobs whose nx is not a multiple of 4. */
+STENCIL_API int stencil_batch_workspace_bytes_for(const stencil_batch_job *jobs, int njobs,
+                                                  size_t *bytes);
 /* Validates the jobs, orders them largest first and writes the job table into
  * d_workspace (256-byte aligned, caller-owned).  cluster_size: CTAs per
  * cluster (1, 2, 4, 8 or 16; 0 = the largest the device schedules; 1 suits

@@ -125,3 +125,50 @@ def test_batch_matches_oracle_and_graph_replay(cuda, cluster_size):
                     (len(shape) == 3 and shape[0] >= 120))
     assert b.kernel_launches() == (1 if c else 0) + w
     b.close()
+
+
+# Ragged sides (nx not a multiple of 4): swept in pitched copies in the batch
+# workspace, one of each engine the batch uses.
+RAGGED = [
+    ((70, 66), 1, 23),            # 2-D, on a cluster from shared memory
+    ((131, 127), 2, 9),           # 2-D, on a cluster
+    ((37, 41, 43), 2, 11),        # 3-D, on a cluster from shared memory
+    ((90, 91, 93), 1, 6),         # 3-D, swept by a cluster from L2
+    ((701, 650), 1, 17),          # 2-D, whole GPU (temporally blocked engine)
+    ((1500, 1301), 1, 5),         # 2-D, whole GPU (rows engine)
+    ((150, 131, 141), 2, 7),      # 3-D, whole GPU (persistent stream kernel)
+    ((64, 64), 1, 12),            # an aligned job in the same batch
+]
+
+
+def test_batch_ragged_sides_match_oracle_and_graph_replay(cuda):
+    import torch
+    from thesis_gb300 import stencil as S
+    hosts, jobs = [], []
+    for k, (shape, radius, iters) in enumerate(RAGGED):
+        u = O.uniform(shape, seed=300 + k)
+        hosts.append(u)
+        jobs.append((torch.from_numpy(u).cuda(), torch.from_numpy(u).cuda(), radius, iters, O.JACOBI))
+    b = S.Batch(jobs)
+    b.launch()
+    torch.cuda.synchronize()
+    wants = []
+    for k, (shape, radius, iters) in enumerate(RAGGED):
+        want, other = oracle_pair(hosts[k], hosts[k], radius, iters, O.JACOBI)
+        wants.append(want)
+        assert bits_equal(b.result(k).cpu().numpy(), want), (k, shape, radius, iters)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            b.launch(stream=s)
+    for k in range(len(RAGGED)):
+        jobs[k][0].copy_(torch.from_numpy(hosts[k]))
+        jobs[k][1].copy_(torch.from_numpy(hosts[k]))
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    for k in range(len(RAGGED)):
+        assert bits_equal(b.result(k).cpu().numpy(), wants[k]), k
+    b.close()
+    assert S.device_status() == 0

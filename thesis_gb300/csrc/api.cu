@@ -103,7 +103,8 @@ static EncodeTiledFn encode_fn() {
 }
 
 int make_tensor_map_typed(CUtensorMap *map, const void *base, int rank, const long long *dims,
-                          const int *box, CUtensorMapDataType dtype, int elem_bytes) {
+                          const int *box, CUtensorMapDataType dtype, int elem_bytes,
+                          long long pitch) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return fail(STENCIL_ECUDA, "cuTensorMapEncodeTiled is unavailable");
     cuuint64_t gdim[3], gstride[2];
@@ -112,8 +113,9 @@ int make_tensor_map_typed(CUtensorMap *map, const void *base, int rank, const lo
         gdim[i] = (cuuint64_t)dims[i];
         bdim[i] = (cuuint32_t)box[i];
     }
-    gstride[0] = (cuuint64_t)dims[0] * elem_bytes;
-    if (rank == 3) gstride[1] = (cuuint64_t)dims[0] * dims[1] * elem_bytes;
+    const long long row = pitch > 0 ? pitch : dims[0];  // row pitch in elements
+    gstride[0] = (cuuint64_t)row * elem_bytes;
+    if (rank == 3) gstride[1] = (cuuint64_t)row * dims[1] * elem_bytes;
     CUresult r = fn(map, dtype, (cuuint32_t)rank, const_cast<void *>(base), gdim, gstride, bdim,
                     estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -142,8 +144,9 @@ int make_tensor_map_general(CUtensorMap *map, CUtensorMapDataType dtype, int ran
 }
 
 int make_tensor_map(CUtensorMap *map, const float *base, int rank, const long long *dims,
-                    const int *box) {
-    return make_tensor_map_typed(map, base, rank, dims, box, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4);
+                    const int *box, long long pitch) {
+    return make_tensor_map_typed(map, base, rank, dims, box, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                                 pitch);
 }
 
 // Per-device scratch kept between calls (host-buffer entry, residual).
@@ -335,7 +338,7 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
     if (variant == STENCIL_VARIANT_COOP && cluster_resident(g, p->dims))
         variant = STENCIL_VARIANT_CLUSTER;
     if (variant == STENCIL_VARIANT_CLUSTER) {
-        if (cluster_shape_ok(p->dims, g.nx, g.ny, g.radius)) {
+        if (cluster_shape_ok(p->dims, (int)g.sy, g.ny, g.radius)) {
             float *res = nullptr;
             rc = run_cluster(g, p->dims, cur, nxt, p->iterations, s, &res);
             if (rc) return rc;

@@ -27,16 +27,18 @@ long long cell_count(const stencil_params &p);
 int num_sms();
 int current_device();
 
-// Builds a tiled TMA descriptor for an FP32 grid (rank 2 or 3).
+// Builds a tiled TMA descriptor for an FP32 grid (rank 2 or 3); pitch: the
+// row pitch in elements when it exceeds dims[0] (0 = dims[0]).
 int make_tensor_map(CUtensorMap *map, const float *base, int rank, const long long *dims,
-                    const int *box);
+                    const int *box, long long pitch = 0);
 // Any rank (1..5), element type, byte strides of dims 1.. and swizzle.
 int make_tensor_map_general(CUtensorMap *map, CUtensorMapDataType dtype, int rank, const void *base,
                             const unsigned long long *dims, const unsigned long long *strides,
                             const unsigned *box, CUtensorMapSwizzle swizzle);
 // The same for another element type (e.g. BF16/FP16 grids, 2 bytes).
 int make_tensor_map_typed(CUtensorMap *map, const void *base, int rank, const long long *dims,
-                          const int *box, CUtensorMapDataType dtype, int elem_bytes);
+                          const int *box, CUtensorMapDataType dtype, int elem_bytes,
+                          long long pitch = 0);
 
 // One sweep per launch kernels (src -> dst).  Each returns a status.
 int launch_base_sweep(const Geom &g, int dims, const float *src, float *dst, int bx, int by,
@@ -78,7 +80,7 @@ int run_cluster(const Geom &g, int dims, float *a, float *b, int iters, cudaStre
 bool cluster_resident(const Geom &g, int dims);
 // The cluster engine takes the shape (nx % 4 == 0, R <= 4, 3-D planes of
 // fewer than 2^31 float4 chunks).
-bool cluster_shape_ok(int dims, int nx, int ny, int radius);
+bool cluster_shape_ok(int dims, int px, int ny, int radius);
 
 // Mixed-precision refinement, persistent 2-D form of an outer step
 // (k_ir2d.cu): one CTA per tile, T correction sweeps per halo exchange.

@@ -41,11 +41,11 @@ namespace st {
 bool tb3d_supported(const Geom &g);
 
 struct ClusterJob {
-    float *a, *b;       // caller buffers (a = initial state)
+    float *a, *b;       // the grid's two buffers (a = initial state)
     int dims, nx, ny, nz;
     int radius, iters, legacy, resident;
     int tblock;         // resident mode: sweeps between halo exchanges (>= 1)
-    int pad;
+    int px;             // row pitch in cells (a multiple of 4, >= nx)
 };
 
 constexpr int kClusterThreads = 512;
@@ -54,16 +54,17 @@ __device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast
 
 // One sweep of the cells of slices [s_begin, s_end) (global slice indices).
 // src/dst address slice s at (s - base) * slice_len; the slice stride is
-// slice_len; within a slice the row pitch is nx.  Rows of the update region
-// only; float4 chunks (nx % 4 == 0 required).  Generic form (any D); used for
-// 2-D rows wider than 4 * blockDim.x cells.
+// slice_len; within a slice the row pitch is px (a multiple of 4; cells nx ..
+// px-1 of a row are padding, read only for cells outside the update region).
+// Rows of the update region only; float4 chunks.  Generic form (any D); used
+// for 2-D rows wider than 4 * blockDim.x cells.
 template <int D, int R>
 __device__ __forceinline__ void sweep_slab(const float *src, float *dst, long long base,
                                            int s_begin, int s_end, const ClusterJob &j) {
     constexpr int C = 2 * D * R;
-    const int nx = j.nx, ny = j.ny;
-    const long long slice_len = D == 3 ? (long long)nx * ny : nx;
-    const int chunks = nx >> 2;
+    const int nx = j.nx, ny = j.ny, px = j.px;
+    const long long slice_len = D == 3 ? (long long)px * ny : px;
+    const int chunks = px >> 2;
     const int rows = D == 3 ? ny - 2 * R : 1;  // update rows per slice
     const int S = D == 3 ? j.nz : ny;
     const int sb = max(s_begin, R), se = min(s_end, S - R);
@@ -76,7 +77,7 @@ __device__ __forceinline__ void sweep_slab(const float *src, float *dst, long lo
         const int s = sb + (int)(rs / rows);
         const int x0 = c * 4;
         if (x0 + 3 < R || x0 >= nx - R) continue;
-        const long long off = (long long)(s - base) * slice_len + (long long)row * nx + x0;
+        const long long off = (long long)(s - base) * slice_len + (long long)row * px + x0;
         const float *p = src + off;
         float w[4 + 2 * ((R + 3) & ~3)];
         constexpr int RA = (R + 3) & ~3;
@@ -95,7 +96,7 @@ __device__ __forceinline__ void sweep_slab(const float *src, float *dst, long lo
             for (int e = 0; e < 4; ++e) acc[e] += w[RA + e + o];
         }
         // axis j: the next row (3-D) or the next slice (2-D)
-        const long long sj = D == 3 ? nx : slice_len;
+        const long long sj = D == 3 ? px : slice_len;
 #pragma unroll
         for (int o = -R; o <= R; ++o) {
             if (!o) continue;
@@ -132,13 +133,13 @@ __device__ __forceinline__ void sweep_slab(const float *src, float *dst, long lo
 // float4 chunk c of every row in it.  The chunk's column of the rows j-R ..
 // j+R rides in a register queue down the block (one new 16-byte load per
 // row); only the x-neighbour chunks are loaded per row.  No index division in
-// the loop.  Requires nx / 4 <= blockDim.x.
+// the loop.  Requires px / 4 <= blockDim.x.
 template <int R>
 __device__ __forceinline__ void sweep_rows2d(const float *src, float *dst, long long base,
                                              int s_begin, int s_end, const ClusterJob &j) {
     constexpr int C = 4 * R;
     constexpr int RA = (R + 3) & ~3;
-    const int nx = j.nx, ny = j.ny, chunks = nx >> 2;
+    const int nx = j.nx, ny = j.ny, px = j.px, chunks = px >> 2;
     const int G = blockDim.x / chunks;
     const int c = threadIdx.x % chunks, grp = threadIdx.x / chunks;
     const int rb = max(s_begin, R), re = min(s_end, ny - R);
@@ -152,15 +153,15 @@ __device__ __forceinline__ void sweep_rows2d(const float *src, float *dst, long 
     for (int e = 0; e < 4; ++e)
         if (x0 + e >= R && x0 + e < nx - R) mask |= 1u << e;
     if (!mask) return;
-    const float *col = src + (long long)(-base) * nx + x0;  // row j of this chunk at col + j*nx
-    float *dcol = dst + (long long)(-base) * nx + x0;
+    const float *col = src + (long long)(-base) * px + x0;  // row j of this chunk at col + j*px
+    float *dcol = dst + (long long)(-base) * px + x0;
     float4 q[2 * R + 1];  // rows j-R .. j+R of this chunk
 #pragma unroll
-    for (int k = 0; k < 2 * R; ++k) q[k] = ld4(col + (long long)(j0 - R + k) * nx);
+    for (int k = 0; k < 2 * R; ++k) q[k] = ld4(col + (long long)(j0 - R + k) * px);
 #pragma unroll 2
     for (int jj = j0; jj < j1; ++jj) {
-        q[2 * R] = ld4(col + (long long)(jj + R) * nx);
-        const float *row = col + (long long)jj * nx;
+        q[2 * R] = ld4(col + (long long)(jj + R) * px);
+        const float *row = col + (long long)jj * px;
         float w[4 + 2 * RA];
 #pragma unroll
         for (int h = 0; h < RA / 4; ++h) {
@@ -192,7 +193,7 @@ __device__ __forceinline__ void sweep_rows2d(const float *src, float *dst, long 
             out[e] = div_coeff<C>(acc[e]);
             if (j.legacy) out[e] -= w[RA + e];
         }
-        float *d = dcol + (long long)jj * nx;
+        float *d = dcol + (long long)jj * px;
         if (mask == 0xFu) {
             *reinterpret_cast<float4 *>(d) = make_float4(out[0], out[1], out[2], out[3]);
         } else {
@@ -224,8 +225,8 @@ __device__ __forceinline__ void sweep_cols3d(const float *src, float *dst, long 
     constexpr int C = 6 * R;
     constexpr int RA = (R + 3) & ~3;
     static_assert(RA == 4, "one neighbour chunk per side");
-    const int nx = j.nx, ny = j.ny, chunks = nx >> 2;
-    const long long sl = (long long)nx * ny;
+    const int nx = j.nx, ny = j.ny, px = j.px, chunks = px >> 2;
+    const long long sl = (long long)px * ny;
     const int rows = ny - 2 * R;
     const int sb = max(s_begin, R), se = min(s_end, j.nz - R);
     if (sb >= se || rows <= 0) return;
@@ -238,7 +239,7 @@ __device__ __forceinline__ void sweep_cols3d(const float *src, float *dst, long 
         for (int e = 0; e < 4; ++e)
             if (x0 + e >= R && x0 + e < nx - R) mask |= 1u << e;
         if (!mask) continue;
-        const long long off = (long long)(sb - base) * sl + (long long)row * nx + x0;
+        const long long off = (long long)(sb - base) * sl + (long long)row * px + x0;
         const float *col = src + off;  // slice sb of this column
         float *dcol = dst + off;
         const bool has_l = c > 0, has_r = c + 1 < chunks;
@@ -253,7 +254,7 @@ __device__ __forceinline__ void sweep_cols3d(const float *src, float *dst, long 
             if (has_r) nr = ld4(col + 4);
 #pragma unroll
             for (int o = -R; o <= R; ++o)
-                if (o) nyv[o < 0 ? o + R : o + R - 1] = ld4(col + o * nx);
+                if (o) nyv[o < 0 ? o + R : o + R - 1] = ld4(col + o * px);
         }
 #pragma unroll 2
         for (int s = sb; s < se; ++s) {
@@ -271,7 +272,7 @@ __device__ __forceinline__ void sweep_cols3d(const float *src, float *dst, long 
                     if (has_r) nr = ld4(nc + 4);
 #pragma unroll
                     for (int o = -R; o <= R; ++o)
-                        if (o) nyv[o < 0 ? o + R : o + R - 1] = ld4(nc + o * nx);
+                        if (o) nyv[o < 0 ? o + R : o + R - 1] = ld4(nc + o * px);
                 }
             } else {
                 q[2 * R] = ld4(col + R * sl);
@@ -279,7 +280,7 @@ __device__ __forceinline__ void sweep_cols3d(const float *src, float *dst, long 
                 r4 = has_r ? ld4(col + 4) : z4;
 #pragma unroll
                 for (int o = -R; o <= R; ++o)
-                    if (o) yv[o < 0 ? o + R : o + R - 1] = ld4(col + o * nx);
+                    if (o) yv[o < 0 ? o + R : o + R - 1] = ld4(col + o * px);
             }
             const float4 m4 = q[R];
             const float w[12] = {l4.x, l4.y, l4.z, l4.w, m4.x, m4.y, m4.z, m4.w, r4.x, r4.y, r4.z, r4.w};
@@ -330,7 +331,7 @@ __device__ __forceinline__ void copy_slices(float *to, const float *from, long l
 template <int D, int R>
 __device__ void run_job(const ClusterJob &j, float *smem, uint32_t rank, uint32_t csize) {
     const int S = D == 3 ? j.nz : j.ny;
-    const long long slice_len = D == 3 ? (long long)j.nx * j.ny : j.nx;
+    const long long slice_len = D == 3 ? (long long)j.px * j.ny : j.px;
     const int H = (S + csize - 1) / csize;
     const int s0 = min((int)rank * H, S), s1 = min(s0 + H, S);
     if (j.resident) {
@@ -359,7 +360,7 @@ __device__ void run_job(const ClusterJob &j, float *smem, uint32_t rank, uint32_
                 if (s1 > s0) {
                     if constexpr (D == 3)
                         sweep_cols3d<R, false>(buf[cur], buf[cur ^ 1], s0 - HT, a, b, j);
-                    else if ((j.nx >> 2) <= (int)blockDim.x)
+                    else if ((j.px >> 2) <= (int)blockDim.x)
                         sweep_rows2d<R>(buf[cur], buf[cur ^ 1], s0 - HT, a, b, j);
                     else
                         sweep_slab<D, R>(buf[cur], buf[cur ^ 1], s0 - HT, a, b, j);
@@ -403,7 +404,7 @@ __device__ void run_job(const ClusterJob &j, float *smem, uint32_t rank, uint32_
         for (int it = 0; it < j.iters; ++it) {
             if constexpr (D == 3)
                 sweep_cols3d<R, (R <= 2)>(src, dst, 0, s0, s1, j);  // R >= 3: no register room
-            else if ((j.nx >> 2) <= (int)blockDim.x)
+            else if ((j.px >> 2) <= (int)blockDim.x)
                 sweep_rows2d<R>(src, dst, 0, s0, s1, j);
             else
                 sweep_slab<D, R>(src, dst, 0, s0, s1, j);
@@ -470,16 +471,16 @@ constexpr int kClusterSmemMax = 200 * 1024;
 
 static long long slab_bytes(const ClusterJob &j, int csize, int tblock) {
     const int S = j.dims == 3 ? j.nz : j.ny;
-    const long long slice_len = j.dims == 3 ? (long long)j.nx * j.ny : j.nx;
+    const long long slice_len = j.dims == 3 ? (long long)j.px * j.ny : j.px;
     const int H = (S + csize - 1) / csize;
     return 2LL * (H + 2 * tblock * j.radius) * slice_len * 4;
 }
 
-// The cluster sweeps read float4 chunks and number a plane's chunk columns
-// with 32-bit integers.
-bool cluster_shape_ok(int dims, int nx, int ny, int radius) {
-    return nx % 4 == 0 && radius >= 1 && radius <= 4 &&
-           (dims == 2 || (long long)(nx / 4) * ny < (1LL << 31));
+// The cluster sweeps read float4 chunks of rows with pitch px and number a
+// plane's chunk columns with 32-bit integers.
+bool cluster_shape_ok(int dims, int px, int ny, int radius) {
+    return px % 4 == 0 && radius >= 1 && radius <= 4 &&
+           (dims == 2 || (long long)(px / 4) * ny < (1LL << 31));
 }
 
 bool cluster_job_ok(int dims, int nx, int ny, int nz, int radius) {
@@ -498,7 +499,6 @@ static void plan_job(ClusterJob &j, int csize, int tmax = 0) {
     const int last = S - ((S + H - 1) / H - 1) * H;
     j.resident = 0;
     j.tblock = 1;
-    j.pad = 0;
     for (int tb : {8, 4, 2, 1}) {
         if (tmax > 0 ? tb > tmax : tb > 4) continue;
         const int ht = tb * j.radius;
@@ -605,6 +605,7 @@ ClusterJob make_job(const Geom &g, int dims, float *a, float *b, int iters, int 
     j.radius = g.radius;
     j.iters = iters;
     j.legacy = g.legacy;
+    j.px = (int)g.sy;
     plan_job(j, csize, tmax);
     return j;
 }
@@ -614,7 +615,7 @@ size_t cluster_job_size() { return sizeof(ClusterJob); }
 // Single grid on one cluster, all sweeps in one launch (queue-less mode).
 int run_cluster(const Geom &g, int dims, float *a, float *b, int iters, cudaStream_t s,
                 float **res) {
-    if (!cluster_shape_ok(dims, g.nx, g.ny, g.radius))
+    if (!cluster_shape_ok(dims, (int)g.sy, g.ny, g.radius))
         return fail(STENCIL_EUNSUPPORTED,
                     "cluster engine needs nx %% 4 == 0, R <= 4 and (3-D) nx/4 * ny < 2^31");
     const int csize = cluster_size_for_device();
@@ -644,7 +645,7 @@ int run_cluster(const Geom &g, int dims, float *a, float *b, int iters, cudaStre
 // Whether a single grid is better served by one cluster than by the
 // full-GPU kernels: it fits in the cluster's shared memory.
 bool cluster_resident(const Geom &g, int dims) {
-    if (!cluster_shape_ok(dims, g.nx, g.ny, g.radius)) return false;
+    if (!cluster_shape_ok(dims, (int)g.sy, g.ny, g.radius)) return false;
     ClusterJob j = make_job(g, dims, nullptr, nullptr, 0, cluster_size_for_device());
     return j.resident != 0;
 }
@@ -678,9 +679,20 @@ struct StreamedJob {
     int temporal, tile_x, tile_y;  // tuning hints (0 = the library's choice)
 };
 
+// A job whose width is not a multiple of 4 (its rows are not 16-byte
+// aligned): swept in a copy with the row pitch rounded up to 4 cells, in the
+// caller's workspace, copied in before the batch's kernels and back after.
+struct StagedJob {
+    float *ua, *ub;  // the caller's buffers
+    float *sa, *sb;  // the pitched copies
+    int nx, px;      // width and pitch in cells
+    long long rows;  // rows of the grid (ny * nz)
+};
+
 struct BatchPlan {
     BatchHeader h;                    // the cluster part (njobs = cluster jobs)
     std::vector<StreamedJob> streamed;
+    std::vector<StagedJob> staged;
 };
 
 // Launch plan of each prepared workspace (set by prepare, read by launch).
@@ -714,6 +726,21 @@ size_t batch_bytes(int njobs) {
     return ((sizeof(BatchHeader) + 255) & ~(size_t)255) + (size_t)njobs * sizeof(ClusterJob);
 }
 
+// Bytes of one staged buffer of a job (0 when its rows are 16-byte aligned).
+size_t staged_bytes(const stencil_batch_job &b) {
+    if (b.nx % 4 == 0 || b.nx <= 0 || b.ny <= 0) return 0;
+    const size_t px = ((size_t)b.nx + 3) & ~(size_t)3;
+    const size_t rows = (size_t)b.ny * (b.dims == 3 && b.nz > 0 ? (size_t)b.nz : 1);
+    return (px * rows * sizeof(float) + 255) & ~(size_t)255;
+}
+
+// The job table, then the staged copies (two per ragged job).
+size_t batch_bytes_for(const stencil_batch_job *jobs, int njobs) {
+    size_t n = (batch_bytes(njobs) + 255) & ~(size_t)255;
+    for (int i = 0; i < njobs; ++i) n += 2 * staged_bytes(jobs[i]);
+    return n;
+}
+
 }  // namespace
 
 }  // namespace st
@@ -726,14 +753,23 @@ extern "C" int stencil_batch_workspace_bytes(int njobs, size_t *bytes) {
     return STENCIL_OK;
 }
 
+extern "C" int stencil_batch_workspace_bytes_for(const stencil_batch_job *jobs, int njobs,
+                                                 size_t *bytes) {
+    if (njobs < 0 || (njobs && !jobs) || !bytes) return fail(STENCIL_EINVAL, "bad arguments");
+    *bytes = batch_bytes_for(jobs, njobs);
+    return STENCIL_OK;
+}
+
 extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, int cluster_size,
                                      void *d_workspace, size_t workspace_bytes,
                                      stencil_stream_t stream) {
     if (njobs < 0 || (njobs && !jobs) || !d_workspace)
         return fail(STENCIL_EINVAL, "bad arguments");
-    if (workspace_bytes < batch_bytes(njobs))
-        return fail(STENCIL_EINVAL, "workspace too small: %zu < %zu bytes", workspace_bytes,
-                    batch_bytes(njobs));
+    if (workspace_bytes < batch_bytes_for(jobs, njobs))
+        return fail(STENCIL_EINVAL,
+                    "workspace too small: %zu < %zu bytes (stencil_batch_workspace_bytes_for "
+                    "counts the copies of jobs whose nx is not a multiple of 4)",
+                    workspace_bytes, batch_bytes_for(jobs, njobs));
     if (reinterpret_cast<uintptr_t>(d_workspace) & 255)
         return fail(STENCIL_EINVAL, "workspace must be 256-byte aligned");
     if (cluster_size < 0 || cluster_size > 16 || (cluster_size & (cluster_size - 1)))
@@ -744,6 +780,7 @@ extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, i
     std::vector<ClusterJob> table;
     std::vector<double> work;
     BatchPlan plan;
+    size_t stage_off = (batch_bytes(njobs) + 255) & ~(size_t)255;
     table.reserve(njobs);
     for (int i = 0; i < njobs; ++i) {
         const stencil_batch_job &b = jobs[i];
@@ -756,20 +793,40 @@ extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, i
         if (!b.d_u1 || !b.d_u2 || b.d_u1 == b.d_u2 ||
             ((reinterpret_cast<uintptr_t>(b.d_u1) | reinterpret_cast<uintptr_t>(b.d_u2)) & 15))
             return fail(STENCIL_EINVAL, "job %d: two distinct 16-byte aligned buffers required", i);
-        if (!cluster_job_ok(b.dims, b.nx, b.ny, b.nz, b.radius))
-            return fail(STENCIL_EUNSUPPORTED, "job %d: batch jobs need nx %% 4 == 0 and radius <= 4", i);
+        const int px = (b.nx + 3) & ~3;
+        if (!cluster_job_ok(b.dims, px, b.ny, b.nz, b.radius))
+            return fail(STENCIL_EUNSUPPORTED, "job %d: batch jobs need radius <= 4", i);
         if (b.temporal < 0 || b.tile_x < 0 || b.tile_y < 0 || (b.tile_x % 4) || b.reserved[0] ||
             b.reserved[1] || b.reserved[2])
             return fail(STENCIL_EINVAL,
                         "job %d: temporal, tile_x, tile_y >= 0, tile_x %% 4 == 0, reserved zero", i);
-        const Geom g = make_geom(p);
-        ClusterJob j = make_job(g, p.dims, b.d_u1, b.d_u2, b.iterations, csize, b.temporal);
+        Geom g = make_geom(p);
+        float *ga = b.d_u1, *gb = b.d_u2;
+        if (px != b.nx) {
+            // swept in pitched copies in the workspace
+            const size_t sb = staged_bytes(b);
+            StagedJob st;
+            st.ua = b.d_u1;
+            st.ub = b.d_u2;
+            st.sa = reinterpret_cast<float *>(static_cast<char *>(d_workspace) + stage_off);
+            st.sb = reinterpret_cast<float *>(static_cast<char *>(d_workspace) + stage_off + sb);
+            st.nx = b.nx;
+            st.px = px;
+            st.rows = (long long)b.ny * (b.dims == 3 ? b.nz : 1);
+            stage_off += 2 * sb;
+            plan.staged.push_back(st);
+            ga = st.sa;
+            gb = st.sb;
+            g.sy = px;
+            g.sz = (long long)px * b.ny;
+        }
+        ClusterJob j = make_job(g, p.dims, ga, gb, b.iterations, csize, b.temporal);
         // small non-resident 3-D grids stay on clusters, many at a time: a
         // whole-GPU launch of one of them is latency-bound
         const bool big3d = (long long)cell_count(p) >= kStreamMinCells3d;
         if (!j.resident && ((p.dims == 3 && big3d && stream3d_supported(g)) ||
                             (p.dims == 2 && rows2d_supported(g, 2)))) {
-            plan.streamed.push_back({g, b.d_u1, b.d_u2, b.iterations, p.dims, b.temporal, b.tile_x,
+            plan.streamed.push_back({g, ga, gb, b.iterations, p.dims, b.temporal, b.tile_x,
                                      b.tile_y});
             continue;
         }
@@ -807,6 +864,12 @@ extern "C" int stencil_batch_launch(const void *d_workspace, stencil_stream_t st
     if (!recall(d_workspace, &plan))
         return fail(STENCIL_EINVAL, "workspace was not prepared by stencil_batch_prepare");
     const BatchHeader &h = plan.h;
+    for (const StagedJob &st : plan.staged) {
+        ST_CUDA(cudaMemcpy2DAsync(st.sa, st.px * sizeof(float), st.ua, st.nx * sizeof(float),
+                                  st.nx * sizeof(float), st.rows, cudaMemcpyDeviceToDevice, s));
+        ST_CUDA(cudaMemcpy2DAsync(st.sb, st.px * sizeof(float), st.ub, st.nx * sizeof(float),
+                                  st.nx * sizeof(float), st.rows, cudaMemcpyDeviceToDevice, s));
+    }
     if (h.njobs) {
         const size_t hb = (sizeof(BatchHeader) + 255) & ~(size_t)255;
         const ClusterJob *table = reinterpret_cast<const ClusterJob *>(static_cast<const char *>(d_workspace) + hb);
@@ -816,15 +879,30 @@ extern "C" int stencil_batch_launch(const void *d_workspace, stencil_stream_t st
     }
     for (const StreamedJob &j : plan.streamed) {
         int rc;
-        if (j.dims == 3)
-            rc = (j.temporal >= 2 && !j.g.legacy && tb3d_supported(j.g))
-                     ? run_tb3d(j.g, j.a, j.b, j.iters, j.temporal, s, nullptr)
-                     : run_stream3d(j.g, j.a, j.b, j.iters, 0, 0, s, nullptr, 0, true);
-        else
+        if (j.dims == 3 && j.temporal >= 2 && !j.g.legacy && j.g.sy == j.g.nx && tb3d_supported(j.g)) {
+            // temporally blocked passes leave the result where the pass count
+            // puts it; the batch keeps the ping-pong loop's place (d_u1 for
+            // an even sweep count, d_u2 for an odd one)
+            float *out = nullptr;
+            rc = run_tb3d(j.g, j.a, j.b, j.iters, j.temporal, s, &out);
+            float *want = (j.iters & 1) ? j.b : j.a;
+            if (!rc && out != want)
+                ST_CUDA(cudaMemcpyAsync(want, out, (size_t)j.g.sz * j.g.nz * sizeof(float),
+                                        cudaMemcpyDeviceToDevice, s));
+        } else if (j.dims == 3) {
+            rc = run_stream3d(j.g, j.a, j.b, j.iters, 0, 0, s, nullptr, 0, true);
+        } else {
             rc = tb2d_supported(j.g, 2)
                      ? run_tb2d(j.g, j.a, j.b, j.iters, j.temporal, j.tile_x, j.tile_y, s, nullptr)
                      : run_rows2d(j.g, j.a, j.b, j.iters, s, nullptr);
+        }
         if (rc) return rc;
+    }
+    for (const StagedJob &st : plan.staged) {
+        ST_CUDA(cudaMemcpy2DAsync(st.ua, st.nx * sizeof(float), st.sa, st.px * sizeof(float),
+                                  st.nx * sizeof(float), st.rows, cudaMemcpyDeviceToDevice, s));
+        ST_CUDA(cudaMemcpy2DAsync(st.ub, st.nx * sizeof(float), st.sb, st.px * sizeof(float),
+                                  st.nx * sizeof(float), st.rows, cudaMemcpyDeviceToDevice, s));
     }
     return STENCIL_OK;
 }

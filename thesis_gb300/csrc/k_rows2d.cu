@@ -40,7 +40,9 @@ __global__ void __launch_bounds__(kRowsThreads, R <= 2 ? 2 : 1)
     constexpr int RA = (R + 3) & ~3;  // x halo in whole chunks (R <= 4: one chunk)
     static_assert(RA == 4, "one neighbour chunk per side");
     __shared__ int s_ok;
-    const int nx = g.nx, ny = g.ny, nch = nx >> 2;
+    // nx: the width (update region x < nx - R); px: the row pitch (a
+    // multiple of 4, the chunk columns cover it)
+    const int nx = g.nx, ny = g.ny, px = (int)g.sy, nch = px >> 2;
     const int items = nch * nblk;
     for (int sw = 0; sw < iters; ++sw) {
         const float *src = (sw & 1) ? b : a;
@@ -56,19 +58,19 @@ __global__ void __launch_bounds__(kRowsThreads, R <= 2 ? 2 : 1)
             float *dcol = dst + x0;
             float4 q[2 * R + 1];  // rows j-R .. j+R of this chunk column
 #pragma unroll
-            for (int k = 0; k < 2 * R; ++k) q[k] = rows_ld4(col + (long long)(j0 - R + k) * nx);
+            for (int k = 0; k < 2 * R; ++k) q[k] = rows_ld4(col + (long long)(j0 - R + k) * px);
             // the loads of row j+1 are issued before row j is computed (one
             // row of software pipelining: two rows of loads in flight)
             const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-            float4 nq = rows_ld4(col + (long long)(j0 + R) * nx);
-            float4 nl = c > 0 ? rows_ld4(col + (long long)j0 * nx - 4) : z4;
-            float4 nr = c + 1 < nch ? rows_ld4(col + (long long)j0 * nx + 4) : z4;
+            float4 nq = rows_ld4(col + (long long)(j0 + R) * px);
+            float4 nl = c > 0 ? rows_ld4(col + (long long)j0 * px - 4) : z4;
+            float4 nr = c + 1 < nch ? rows_ld4(col + (long long)j0 * px + 4) : z4;
             for (int j = j0; j < j1; ++j) {
                 q[2 * R] = nq;
                 const float4 l4 = nl, r4 = nr;
                 if (j + 1 < j1) {
-                    const float *nrow = col + (long long)(j + 1) * nx;
-                    nq = rows_ld4(col + (long long)(j + 1 + R) * nx);
+                    const float *nrow = col + (long long)(j + 1) * px;
+                    nq = rows_ld4(col + (long long)(j + 1 + R) * px);
                     if (c > 0) nl = rows_ld4(nrow - 4);
                     if (c + 1 < nch) nr = rows_ld4(nrow + 4);
                 }
@@ -94,7 +96,7 @@ __global__ void __launch_bounds__(kRowsThreads, R <= 2 ? 2 : 1)
                     out[e] = div_coeff<C>(acc[e]);
                     if (g.legacy) out[e] -= w[4 + e];
                 }
-                float *d = dcol + (long long)j * nx;
+                float *d = dcol + (long long)j * px;
                 if (full) {
                     *reinterpret_cast<float4 *>(d) = make_float4(out[0], out[1], out[2], out[3]);
                 } else {
@@ -153,17 +155,17 @@ int rows_ctas(int r) {
 }  // namespace
 
 bool rows2d_supported(const Geom &g, int dims) {
-    return dims == 2 && g.nx % 4 == 0 && g.radius >= 1 && g.radius <= 4 &&
-           (long long)(g.nx / 4) * (g.ny - 2 * g.radius) < (1LL << 31) && rows_ctas(g.radius) > 0;
+    return dims == 2 && g.sy % 4 == 0 && g.radius >= 1 && g.radius <= 4 &&
+           (long long)(g.sy / 4) * (g.ny - 2 * g.radius) < (1LL << 31) && rows_ctas(g.radius) > 0;
 }
 
 int run_rows2d(const Geom &g, float *a, float *b, int iters, cudaStream_t s, float **res) {
     if (!rows2d_supported(g, 2))
-        return fail(STENCIL_EUNSUPPORTED, "persistent 2-D rows kernel: nx %% 4 == 0, R <= 4");
+        return fail(STENCIL_EUNSUPPORTED, "persistent 2-D rows kernel: row pitch %% 4 == 0, R <= 4");
     if (res) *res = (iters & 1) ? b : a;
     if (iters <= 0) return STENCIL_OK;
     const int ctas = rows_ctas(g.radius);
-    const int nch = g.nx / 4, rows = g.ny - 2 * g.radius;
+    const int nch = (int)(g.sy / 4), rows = g.ny - 2 * g.radius;
     // Row blocks as tall as keeps about four items per resident thread (a
     // taller block re-reads fewer halo rows), at most 64 rows and at least 4
     // (R = 1) or 8 rows (measured on 1024^2 to 32768^2 grids).

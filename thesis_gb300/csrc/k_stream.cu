@@ -457,7 +457,7 @@ int kernel_residency(const void *fn, int threads, int smem, int *per_sm) {
 }  // namespace
 
 bool stream3d_supported(const Geom &g) {
-    return g.nx % 4 == 0 && (g.radius >= 1 && g.radius <= 4);
+    return g.sy % 4 == 0 && (g.radius >= 1 && g.radius <= 4);
 }
 
 int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int tile_y,
@@ -480,7 +480,7 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     if (!k.fn) return fail(STENCIL_EUNSUPPORTED, "stream kernel has no radius-%d instance", R);
     if (persistent && !k.multi)
         return fail(STENCIL_EUNSUPPORTED, "the persistent stream kernel exists for the default shapes only");
-    if (g.nx % 4) return fail(STENCIL_EUNSUPPORTED, "stream kernel needs nx %% 4 == 0");
+    if (g.sy % 4) return fail(STENCIL_EUNSUPPORTED, "stream kernel needs a row pitch %% 4 == 0");
     const void *fn = persistent ? k.multi : k.fn;
     int per_sm = 0;
     int rc = kernel_residency(fn, k.threads, k.smem, &per_sm);
@@ -517,8 +517,8 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     CUtensorMap maps[2];
     const long long dims[3] = {g.nx, g.ny, g.nz};
     const int box[3] = {k.tx + 2 * ((R + 3) & ~3), k.ty + 2 * R, 1};
-    rc = make_tensor_map(&maps[0], a, 3, dims, box);
-    if (!rc) rc = make_tensor_map(&maps[1], b, 3, dims, box);
+    rc = make_tensor_map(&maps[0], a, 3, dims, box, g.sy);
+    if (!rc) rc = make_tensor_map(&maps[1], b, 3, dims, box, g.sy);
     if (rc) return rc;
     Geom gg = g;
     int tx_ = tiles_x, ty_ = tiles_y, it_ = items;

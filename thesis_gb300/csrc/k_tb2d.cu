@@ -109,17 +109,20 @@ template <int R, bool LEGACY, int NI>
 __global__ void __launch_bounds__(kTb2Threads, 1)
     k_tb2d(float *g0, float *g1, Geom g, Tb2Plan p, int iters, unsigned long long *xch) {
     extern __shared__ __align__(16) float tb2_smem[];
-    const int nx = g.nx, ny = g.ny, pw = p.pw;
+    // nx: the grid's width (update region x < nx - R); px: its row pitch (a
+    // multiple of 4; cells nx .. px-1 of a row are padding that no update
+    // reads and no sweep writes)
+    const int nx = g.nx, ny = g.ny, px = (int)g.sy, pw = p.pw;
     float *const S0 = tb2_smem, *const S1 = tb2_smem + pw * p.ph;
     const int tile = blockIdx.x, ntiles = p.tiles_x * p.tiles_y;
     const int x0 = (tile % p.tiles_x) * p.tx, y0 = (tile / p.tiles_x) * p.ty;
     const int ox = x0 - p.hx, oy = y0 - p.hy;  // grid coordinates of local (0, 0)
-    const int x1 = min(x0 + p.tx, nx), y1 = min(y0 + p.ty, ny);  // owned tile end
+    const int x1 = min(x0 + p.tx, px), y1 = min(y0 + p.ty, ny);  // owned tile end
     const size_t tile_words = (size_t)p.tx * p.ty;
     // two sweeps or more: at least two blocks (see the header)
     const int T = iters >= 2 ? min(p.t, iters - 1) : 1;
     // The extended tile clipped to the grid.
-    const int exa = max(ox, 0), exb = min(ox + pw, nx);
+    const int exa = max(ox, 0), exb = min(ox + pw, px);
     const int eya = max(oy, 0), eyb = min(oy + p.ph, ny);
 
     // This thread's float4 chunks of the extended tile, fixed for the launch
@@ -191,7 +194,7 @@ __global__ void __launch_bounds__(kTb2Threads, 1)
         const int n = cw * (eyb - eya);
         for (int u = threadIdx.x; u < n; u += kTb2Threads) {
             const int y = eya + u / cw, x = exa + 4 * (u % cw);
-            const long long gi = (long long)y * nx + x;
+            const long long gi = (long long)y * px + x;
             const int si = (y - oy) * pw + (x - ox);
             *reinterpret_cast<float4 *>(S0 + si) = __ldcg(reinterpret_cast<const float4 *>(g0 + gi));
             if (y < R || y >= ny - R) {
@@ -301,7 +304,7 @@ __global__ void __launch_bounds__(kTb2Threads, 1)
         for (int u = threadIdx.x; u < n; u += kTb2Threads) {
             const int y = ya + u / cw, x = x0 + 4 * (u % cw);
             const int si = (y - oy) * pw + (x - ox);
-            const long long gi = (long long)y * nx + x;
+            const long long gi = (long long)y * px + x;
             const float4 vn = tb2_ld4(Sn + si), vp = tb2_ld4(Sp + si);
             if (x >= R && x + 3 < nx - R) {
                 __stcg(reinterpret_cast<float4 *>(Gn + gi), vn);
@@ -358,7 +361,7 @@ bool make_plan(const Geom &g, int t, int tx, int ty, int max_ctas, Tb2Plan *p) {
     q.hy = t * R;
     q.pw = tx + 2 * q.hx;
     q.ph = ty + 2 * q.hy;
-    q.tiles_x = (g.nx + tx - 1) / tx;
+    q.tiles_x = ((int)g.sy + tx - 1) / tx;  // tiles cover the row pitch
     q.tiles_y = (g.ny + ty - 1) / ty;
     if ((long long)q.tiles_x * q.tiles_y > max_ctas) return false;
     // the halo reaches the adjacent tiles only
@@ -405,7 +408,7 @@ bool choose_plan(const Geom &g, int iters, int temporal, int tile_x, int tile_y,
     // two sweeps or more take at least two blocks (see the kernel)
     const int tmax = iters >= 2 ? std::min(iters - 1, 31) : 1;
     if (temporal > 0) temporal = std::min(temporal, tmax);
-    const Key key = {g.nx, g.ny, g.radius, tmax, temporal, tile_x, tile_y, max_ctas};
+    const Key key = {(int)g.sy, g.ny, g.radius, tmax, temporal, tile_x, tile_y, max_ctas};
     std::lock_guard<std::mutex> lock(mu);
     for (auto &c : cache)
         if (c.first == key) {
@@ -522,7 +525,7 @@ void tb2d_release() {
 }
 
 bool tb2d_supported(const Geom &g, int dims) {
-    if (dims != 2 || g.nx % 4 || g.radius < 1 || g.radius > 4) return false;
+    if (dims != 2 || g.sy % 4 || g.radius < 1 || g.radius > 4) return false;
     const int ctas = tb2_max_ctas(g.radius);
     Tb2Plan p;
     return ctas > 0 && choose_plan(g, 1, 1, 0, 0, ctas, &p);
@@ -530,8 +533,8 @@ bool tb2d_supported(const Geom &g, int dims) {
 
 int run_tb2d(const Geom &g, float *a, float *b, int iters, int temporal, int tile_x, int tile_y,
              cudaStream_t s, float **res) {
-    if (g.nx % 4 || g.radius < 1 || g.radius > 4)
-        return fail(STENCIL_EUNSUPPORTED, "2-D temporal blocking needs nx %% 4 == 0 and R <= 4");
+    if (g.sy % 4 || g.radius < 1 || g.radius > 4)
+        return fail(STENCIL_EUNSUPPORTED, "2-D temporal blocking needs a row pitch %% 4 == 0 and R <= 4");
     const int ctas = tb2_max_ctas(g.radius);
     Tb2Plan p;
     // a caller tile that does not fit falls back to the library's choice

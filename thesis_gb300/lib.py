@@ -116,6 +116,7 @@ def load() -> ctypes.CDLL:
                                      ctypes.POINTER(ctypes.c_uint)]),
         "stencil_selftest_wait": (i, [i, ctypes.POINTER(i), ctypes.POINTER(i)]),
         "stencil_batch_workspace_bytes": (i, [i, ctypes.POINTER(sz)]),
+        "stencil_batch_workspace_bytes_for": (i, [ctypes.POINTER(BatchJob), i, ctypes.POINTER(sz)]),
         "stencil_batch_prepare": (i, [ctypes.POINTER(BatchJob), i, i, vp, sz, vp]),
         "stencil_batch_launch": (i, [vp, vp]),
         "stencil_batch_forget": (i, [vp]),

@@ -264,8 +264,8 @@ class Batch:
             j.radius, j.iterations, j.mode = radius, iters, mode
         L = _lib.load()
         nbytes = ctypes.c_size_t()
-        _lib.check(L.stencil_batch_workspace_bytes(len(self.jobs), ctypes.byref(nbytes)),
-                   "stencil_batch_workspace_bytes")
+        _lib.check(L.stencil_batch_workspace_bytes_for(arr, len(self.jobs), ctypes.byref(nbytes)),
+                   "stencil_batch_workspace_bytes_for")
         dev = self.jobs[0][0].device if self.jobs else torch.device("cuda")
         self.workspace = torch.empty(nbytes.value + 256, dtype=torch.uint8, device=dev)
         base = self.workspace.data_ptr()
