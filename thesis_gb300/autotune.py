@@ -291,9 +291,9 @@ def tune_batch(make_jobs, classes=None, repeats=2, log=print):
             hint = {"temporal": cfg.get("temporal", 0), "tile": tuple(cfg.get("tile", (0, 0)))}
             best = float("inf")
             for _ in range(repeats):
-                for (u1, u2), (a, b) in zip(init, jobs):
-                    a.copy_(u1)
-                    b.copy_(u2)
+                for (u1, u2), job in zip(init, jobs):
+                    job[0].copy_(u1)
+                    job[1].copy_(u2)
                 try:
                     bt = S.Batch([tuple(j[:5]) + (hint,) for j in jobs])
                 except _lib.StencilError:

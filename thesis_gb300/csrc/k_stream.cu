@@ -475,7 +475,13 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     int shape = (!tile_x && !tile_y) ? (R <= 2 ? 3 : 4)
                                      : (tile_y == 1 ? 2 : ((tile_x && tile_x < 128) || tile_y > 16 ? 1 : 0));
     if (shape_hint >= 1 && shape_hint <= 6) shape = shape_hint;
-    if (persistent && !(shape_hint >= 1 && shape_hint <= 6)) shape = R == 1 ? 3 : (R == 2 ? 5 : 4);
+    // Persistent default per radius; at R = 2 on large grids (2^25 cells and
+    // up) the same shape with x neighbours by warp shuffles (GB300, same box:
+    // 512^3 694 vs 631 GCell/s, 384^3 653 vs 636; on 256^3 and smaller the
+    // shared-memory reads win: 525 vs 605 at 256^3, 258 vs 301 at 128^3).
+    const bool big = (long long)g.nx * g.ny * g.nz >= (1LL << 25);
+    if (persistent && !(shape_hint >= 1 && shape_hint <= 6))
+        shape = R == 1 ? 3 : (R == 2 ? (big ? 6 : 5) : 4);
     StreamKernel k = pick(R, shape);
     if (!k.fn) return fail(STENCIL_EUNSUPPORTED, "stream kernel has no radius-%d instance", R);
     if (persistent && !k.multi)
