@@ -196,19 +196,33 @@ STENCIL_API int stencil_batch_workspace_bytes_for(const stencil_batch_job *jobs,
 STENCIL_API int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, int cluster_size,
                                       void *d_workspace, size_t workspace_bytes,
                                       stencil_stream_t stream);
-/* Runs the prepared jobs: one persistent cluster launch over a device work
- * queue (every cluster the device can hold) for the jobs that a cluster
- * sweeps, then, for each job too large for a cluster's shared memory, one
- * persistent whole-GPU launch.  Resets the queue counter first.
- * Asynchronous; allocates nothing; can be captured into a CUDA graph (the
- * queue reset is a memset node, so every replay runs the whole batch
- * again). */
+/* Runs the prepared jobs: the copies of ragged jobs in (one kernel), one
+ * persistent cluster launch over a device work queue (every cluster the
+ * device can hold) for the jobs that a cluster sweeps, then, for each job too
+ * large for a cluster's shared memory, one persistent launch of its own, and
+ * the copies out.  Those launches run on the whole GPU, except that mid-size
+ * 3-D jobs (below 2^25 cells) of one radius and mode run in lanes side by
+ * side, each lane a queue of jobs on its share of the CTAs the device holds
+ * (jobs assigned largest first to the lane with the least work), all lanes
+ * but the first on streams that prepare creates for the workspace (forked
+ * from and joined back into `stream` by events).  Environment variables read
+ * by prepare override the defaults: STENCIL_BATCH_LANES (4; 1 = no lanes),
+ * STENCIL_BATCH_LANE_MAX_CELLS (2^25; 0 = no lanes) and
+ * STENCIL_BATCH_STREAM_MIN_CELLS_3D (1.2 M: 3-D jobs below it that do not fit
+ * a cluster's shared memory are swept by a cluster from L2).  Resets the queue
+ * counter first.  Asynchronous; allocates nothing; can be captured into a
+ * CUDA graph (the queue reset is a memset node, so every replay runs the
+ * whole batch again; lanes become parallel branches). */
 STENCIL_API int stencil_batch_launch(const void *d_workspace, stencil_stream_t stream);
 /* How stencil_batch_launch runs a prepared workspace: *cluster_jobs jobs in
  * the cluster launch (none: no cluster launch), *whole_gpu_jobs jobs with a
  * launch of their own. */
 STENCIL_API int stencil_batch_plan(const void *d_workspace, int *cluster_jobs, int *whole_gpu_jobs);
-/* Drops the host-side record of a prepared workspace (call before freeing it). */
+/* *groups = how many sets of lanes run side by side (one per radius and
+ * mode), *jobs = the jobs in them. */
+STENCIL_API int stencil_batch_side_by_side(const void *d_workspace, int *groups, int *jobs);
+/* Drops the host-side record of a prepared workspace and its streams (call
+ * before freeing it). */
 STENCIL_API int stencil_batch_forget(const void *d_workspace);
 
 /* ---- Mixed-precision iterative refinement (no counterpart in the reference).

@@ -34,6 +34,9 @@ CASES = [
     ([((720, 704), 1, 33)], {"temporal": 6, "tile": (64, 32)}),             # 2d_large, tb2d hints
     ([((160, 128, 136), 1, 9), ((130, 120, 128), 2, 7)], {"temporal": 2}),  # 3d_large, tb3d
     ([((150, 128, 128), 2, 8)], {"temporal": 3}),                            # 3d_large, tb3d T=3
+    # hints tuned on a smaller grid of the class that do not fit this one
+    # (no tile of depth 16 fits one tile per SM): the library's plan runs
+    ([((1400, 1502), 1, 21)], {"temporal": 16, "tile": (16, 4)}),           # 2d_large, ragged
 ]
 
 

@@ -172,3 +172,73 @@ def test_batch_ragged_sides_match_oracle_and_graph_replay(cuda):
         assert bits_equal(b.result(k).cpu().numpy(), wants[k]), k
     b.close()
     assert S.device_status() == 0
+
+
+# Mid-size 3-D grids too large for the cluster engine: per radius and mode,
+# lanes side by side (each a queue of jobs on its share of the device's
+# CTAs); the LEGACY job has no other job of its kind and runs alone.
+PAIRED = [
+    ((120, 120, 120), 1, 9, "jacobi"),
+    ((130, 128, 136), 1, 8, "jacobi"),
+    ((112, 120, 128), 1, 5, "jacobi"),
+    ((160, 144, 128), 2, 7, "jacobi"),
+    ((150, 131, 141), 2, 6, "jacobi"),      # ragged: swept in a pitched copy
+    ((110, 112, 116), 2, 5, "jacobi"),
+    ((124, 120, 107), 2, 3, "jacobi"),      # ragged
+    ((100, 128, 120), 2, 4, "jacobi"),
+    ((128, 128, 128), 1, 4, "legacy"),
+]
+
+# (STENCIL_BATCH_LANES, STENCIL_BATCH_LANE_MAX_CELLS, expected (lane sets, jobs in them))
+LANES = [("", "", (2, 8)),        # the defaults: 4 lanes below 2^25 cells
+         ("2", "", (2, 8)),       # two lanes, queues of 2 and 1 (R = 1) and 3 and 2 (R = 2)
+         ("8", "", (2, 8)),       # as many lanes as jobs
+         ("1", "", (0, 0)),       # every job alone
+         ("", "0", (0, 0))]
+
+
+@pytest.mark.parametrize("lanes,cap,expect", LANES)
+def test_batch_lanes_mid_size_3d_jobs(cuda, monkeypatch, lanes, cap, expect):
+    import torch
+    from thesis_gb300 import stencil as S
+    monkeypatch.setenv("STENCIL_BATCH_LANES", lanes)
+    monkeypatch.setenv("STENCIL_BATCH_LANE_MAX_CELLS", cap)
+    hosts, jobs, modes = [], [], []
+    for k, (shape, radius, iters, mode) in enumerate(PAIRED):
+        u = O.uniform(shape, seed=400 + k)
+        m = O.JACOBI if mode == "jacobi" else O.LEGACY
+        hosts.append(u)
+        modes.append(m)
+        jobs.append((torch.from_numpy(u).cuda(), torch.from_numpy(u).cuda(), radius, iters, m))
+    b = S.Batch(jobs)
+    assert b.plan() == (0, len(PAIRED))
+    assert b.side_by_side() == expect
+    b.launch()
+    torch.cuda.synchronize()
+    wants = []
+    for k, (shape, radius, iters, _) in enumerate(PAIRED):
+        want, _ = oracle_pair(hosts[k], hosts[k], radius, iters, modes[k])
+        wants.append(want)
+        assert bits_equal(b.result(k).cpu().numpy(), want), (k, shape, radius, iters)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            b.launch(stream=s)
+    for k in range(len(PAIRED)):
+        jobs[k][0].copy_(torch.from_numpy(hosts[k]))
+        jobs[k][1].copy_(torch.from_numpy(hosts[k]))
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    # a second replay from reset inputs (the barrier counters are reused)
+    for k in range(len(PAIRED)):
+        jobs[k][0].copy_(torch.from_numpy(hosts[k]))
+        jobs[k][1].copy_(torch.from_numpy(hosts[k]))
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    for k in range(len(PAIRED)):
+        assert bits_equal(b.result(k).cpu().numpy(), wants[k]), k
+    b.close()
+    assert S.device_status() == 0

@@ -104,7 +104,7 @@ static EncodeTiledFn encode_fn() {
 
 int make_tensor_map_typed(CUtensorMap *map, const void *base, int rank, const long long *dims,
                           const int *box, CUtensorMapDataType dtype, int elem_bytes,
-                          long long pitch) {
+                          long long pitch, bool nan_fill) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return fail(STENCIL_ECUDA, "cuTensorMapEncodeTiled is unavailable");
     cuuint64_t gdim[3], gstride[2];
@@ -118,7 +118,9 @@ int make_tensor_map_typed(CUtensorMap *map, const void *base, int rank, const lo
     if (rank == 3) gstride[1] = (cuuint64_t)row * dims[1] * elem_bytes;
     CUresult r = fn(map, dtype, (cuuint32_t)rank, const_cast<void *>(base), gdim, gstride, bdim,
                     estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    nan_fill ? CU_TENSOR_MAP_FLOAT_OOB_FILL_NAN_REQUEST_ZERO_FMA
+                             : CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(STENCIL_EINVAL, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return STENCIL_OK;
 }
@@ -144,9 +146,9 @@ int make_tensor_map_general(CUtensorMap *map, CUtensorMapDataType dtype, int ran
 }
 
 int make_tensor_map(CUtensorMap *map, const float *base, int rank, const long long *dims,
-                    const int *box, long long pitch) {
+                    const int *box, long long pitch, bool nan_fill) {
     return make_tensor_map_typed(map, base, rank, dims, box, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
-                                 pitch);
+                                 pitch, nan_fill);
 }
 
 // Per-device scratch kept between calls (host-buffer entry, residual).

@@ -28,9 +28,10 @@ int num_sms();
 int current_device();
 
 // Builds a tiled TMA descriptor for an FP32 grid (rank 2 or 3); pitch: the
-// row pitch in elements when it exceeds dims[0] (0 = dims[0]).
+// row pitch in elements when it exceeds dims[0] (0 = dims[0]).  Box cells
+// outside the grid read as zeros, or as NaN with nan_fill.
 int make_tensor_map(CUtensorMap *map, const float *base, int rank, const long long *dims,
-                    const int *box, long long pitch = 0);
+                    const int *box, long long pitch = 0, bool nan_fill = false);
 // Any rank (1..5), element type, byte strides of dims 1.. and swizzle.
 int make_tensor_map_general(CUtensorMap *map, CUtensorMapDataType dtype, int rank, const void *base,
                             const unsigned long long *dims, const unsigned long long *strides,
@@ -38,7 +39,7 @@ int make_tensor_map_general(CUtensorMap *map, CUtensorMapDataType dtype, int ran
 // The same for another element type (e.g. BF16/FP16 grids, 2 bytes).
 int make_tensor_map_typed(CUtensorMap *map, const void *base, int rank, const long long *dims,
                           const int *box, CUtensorMapDataType dtype, int elem_bytes,
-                          long long pitch = 0);
+                          long long pitch = 0, bool nan_fill = false);
 
 // One sweep per launch kernels (src -> dst).  Each returns a status.
 int launch_base_sweep(const Geom &g, int dims, const float *src, float *dst, int bx, int by,
@@ -54,8 +55,13 @@ void note_launches(const char *engine, long long n);
 bool stream3d_supported(const Geom &g);
 // persistent: all sweeps in one cooperative launch with a grid barrier
 // between sweeps (default shape of each radius) instead of one launch each.
+// max_ctas > 0 caps the CTAs of the launch (the persistent form then keeps
+// its grid barrier over those CTAs only).
 int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int tile_y,
-                 cudaStream_t s, float **res, int shape_hint = 0, bool persistent = false);
+                 cudaStream_t s, float **res, int shape_hint = 0, bool persistent = false,
+                 int max_ctas = 0);
+// CTAs of the device that the persistent stream kernel for g can hold at once.
+int stream3d_capacity(const Geom &g, int *ctas);
 int run_tb3d(const Geom &g, float *a, float *b, int iters, int temporal, cudaStream_t s,
              float **res);
 // A zeroed grid-barrier counter for one persistent launch on stream s

@@ -31,6 +31,8 @@
 // Jobs are ordered by the host (largest first).  Every wait is a hardware
 // cluster barrier: no spin loops.
 #include <algorithm>
+#include <cstdlib>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -681,18 +683,90 @@ struct StreamedJob {
 
 // A job whose width is not a multiple of 4 (its rows are not 16-byte
 // aligned): swept in a copy with the row pitch rounded up to 4 cells, in the
-// caller's workspace, copied in before the batch's kernels and back after.
+// caller's workspace, copied in before the batch's kernels and back after by
+// k_stage (the table of these entries is in the workspace too).
 struct StagedJob {
     float *ua, *ub;  // the caller's buffers
     float *sa, *sb;  // the pitched copies
     int nx, px;      // width and pitch in cells
     long long rows;  // rows of the grid (ny * nz)
+    long long row0;  // rows of the entries before this one
+};
+
+// Copies every staged job's two buffers between the caller's rows (pitch nx)
+// and the pitched copies (pitch px): to the copies when `in`, back otherwise.
+// A warp owns a run of consecutive rows of the concatenated jobs (one search
+// of the table per run) and copies a row with coalesced 4-byte accesses,
+// four per lane in flight.  One launch for all jobs: a 2-D memcpy per buffer
+// pays a fixed cost per row, about 1.2 s per batch for the 3-D grids of the
+// 512-grid benchmark batch.
+constexpr int kStageThreads = 256;
+__global__ void __launch_bounds__(kStageThreads)
+    k_stage(const StagedJob *__restrict__ t, int n, long long total_rows, int rows_per_warp, bool in) {
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * kStageThreads + threadIdx.x) >> 5;
+    long long r = warp * rows_per_warp;
+    const long long r_end = min(r + rows_per_warp, total_rows);
+    if (r >= r_end) return;
+    int lo = 0, hi = n - 1;  // the last entry with row0 <= r
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (t[mid].row0 <= r) lo = mid; else hi = mid - 1;
+    }
+    int j = lo;
+    while (r < r_end) {
+        const StagedJob e = t[j];
+        const long long stop = min(r_end, e.row0 + e.rows);
+        for (; r < stop; ++r) {
+            const long long lr = r - e.row0;
+            for (int h = 0; h < 2; ++h) {
+                const float *src = in ? (h ? e.ub : e.ua) + lr * e.nx : (h ? e.sb : e.sa) + lr * e.px;
+                float *dst = in ? (h ? e.sb : e.sa) + lr * e.px : (h ? e.ub : e.ua) + lr * e.nx;
+                for (int x = lane; x < e.nx; x += 128) {
+                    float v[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (x + 32 * k < e.nx) v[k] = __ldcs(src + x + 32 * k);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (x + 32 * k < e.nx) dst[x + 32 * k] = v[k];
+                }
+            }
+        }
+        ++j;
+    }
+}
+
+// Up to kLanes - 1 extra streams with their fork and join events, owned by
+// one prepared workspace: mid-size 3-D jobs run side by side, one lane on
+// the caller's stream and the others here, each lane a queue of jobs on its
+// share of the CTAs the device holds (a whole-GPU launch of one of them is
+// latency-bound).
+constexpr int kLanes = 8;
+struct Lanes {
+    cudaStream_t s[kLanes - 1] = {};
+    cudaEvent_t fork = nullptr, join[kLanes - 1] = {};
+    ~Lanes() {
+        for (auto &e : join)
+            if (e) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+        for (auto &x : s)
+            if (x) cudaStreamDestroy(x);
+    }
 };
 
 struct BatchPlan {
     BatchHeader h;                    // the cluster part (njobs = cluster jobs)
     std::vector<StreamedJob> streamed;
-    std::vector<StagedJob> staged;
+    int nstaged = 0;                  // staged jobs (their table is in the workspace)
+    long long staged_rows = 0;
+    size_t stage_table = 0;           // workspace offset of the table
+    // the whole-GPU jobs in phases, one after the other: a phase of one lane
+    // runs its jobs in order on the whole GPU; a phase of n > 1 lanes runs
+    // n queues side by side, each job with at most `ctas` CTAs
+    struct Phase { int ctas; std::vector<std::vector<int>> queue; };
+    std::vector<Phase> phases;
+    std::shared_ptr<Lanes> lanes;     // set when some phase has two lanes or more
 };
 
 // Launch plan of each prepared workspace (set by prepare, read by launch).
@@ -716,11 +790,152 @@ bool recall(const void *ws, BatchPlan *h) {
 // 3-D jobs below this many cells (about 106^3) that do not fit a cluster's
 // shared memory are swept by a cluster from L2, several jobs at a time: on
 // the 512-grid batch 3.79 s, against 4.12 s with every such job on the whole
-// GPU (thresholds 0.3 M / 0.7 M / 2.5 M cells: 4.04 / 3.85 / 3.81 s).
+// GPU (thresholds 0.3 M / 0.7 M / 2.5 M cells: 4.04 / 3.85 / 3.81 s).  The
+// environment variable STENCIL_BATCH_STREAM_MIN_CELLS_3D overrides it at
+// prepare time.
 #ifndef STENCIL_STREAM_MIN_CELLS_3D
 #define STENCIL_STREAM_MIN_CELLS_3D 1200000
 #endif
 constexpr long long kStreamMinCells3d = STENCIL_STREAM_MIN_CELLS_3D;
+
+// 3-D whole-GPU jobs below STENCIL_BATCH_LANE_MAX_CELLS cells (2^25, about
+// 320^3) run side by side in STENCIL_BATCH_LANES lanes, each on that share of
+// the device's CTAs; environment variables of the same names override them
+// at prepare time (lanes 1 or cells 0 = never).
+#ifndef STENCIL_BATCH_LANE_MAX_CELLS
+#define STENCIL_BATCH_LANE_MAX_CELLS 33554432
+#endif
+#ifndef STENCIL_BATCH_LANES
+#define STENCIL_BATCH_LANES 4
+#endif
+
+long long env_cells(const char *name, long long dflt) {
+    const char *e = std::getenv(name);
+    if (e && *e) {
+        char *end = nullptr;
+        const long long v = std::strtoll(e, &end, 10);
+        if (end && *end == 0 && v >= 0) return v;
+    }
+    return dflt;
+}
+
+// 3-D jobs swept by the stream kernel (not the temporally blocked one).
+bool stream_job(const StreamedJob &j) {
+    return j.dims == 3 && !(j.temporal >= 2 && !j.g.legacy && j.g.sy == j.g.nx && tb3d_supported(j.g));
+}
+
+long long job_cells(const StreamedJob &j) { return (long long)j.g.nx * j.g.ny * j.g.nz; }
+
+// Orders the whole-GPU jobs into phases.  First every job that runs alone,
+// in the given order; then, per kernel (radius, arithmetic, shape class: the
+// grids' CTAs are then interchangeable on an SM, so all lanes' CTAs fit on
+// the device at once), the mid-size 3-D stream jobs in lanes, each job to the
+// lane with the least work so far, largest first (longest-processing-time
+// scheduling; work = cells x sweeps).
+int plan_phases(BatchPlan *plan) {
+    const long long cap = env_cells("STENCIL_BATCH_LANE_MAX_CELLS", STENCIL_BATCH_LANE_MAX_CELLS);
+    const int lanes = (int)std::min<long long>(kLanes, std::max<long long>(
+        1, env_cells("STENCIL_BATCH_LANES", STENCIL_BATCH_LANES)));
+    const int n = (int)plan->streamed.size();
+    auto work = [&](int i) { return (double)job_cells(plan->streamed[i]) * plan->streamed[i].iters; };
+    auto laned = [&](int i) {
+        const StreamedJob &j = plan->streamed[i];
+        return lanes > 1 && stream_job(j) && job_cells(j) < cap;
+    };
+    // kernel class of a laned job
+    auto kclass = [&](int i) {
+        const StreamedJob &j = plan->streamed[i];
+        return j.g.radius * 4 + (j.g.legacy ? 2 : 0) + (job_cells(j) >= (1LL << 25) ? 1 : 0);
+    };
+    plan->phases.clear();
+    BatchPlan::Phase alone{0, {{}}};
+    std::vector<std::vector<int>> byclass(4 * 5);
+    for (int i = 0; i < n; ++i) {
+        if (laned(i)) byclass[kclass(i)].push_back(i);
+        else alone.queue[0].push_back(i);
+    }
+    for (auto &c : byclass)
+        if (c.size() == 1) {  // nothing to run beside it
+            alone.queue[0].push_back(c[0]);
+            c.clear();
+        }
+    if (!alone.queue[0].empty()) plan->phases.push_back(alone);
+    // A phase's launches take consecutive grid-barrier counters (a ring of
+    // 256): at most 128 jobs per phase keeps the counters of lanes running at
+    // once distinct.
+    constexpr size_t kPhaseJobs = 128;
+    std::vector<std::vector<int>> parts;
+    for (auto &c : byclass) {
+        if (c.empty()) continue;
+        std::stable_sort(c.begin(), c.end(), [&](int x, int y) { return work(x) > work(y); });
+        for (size_t k = 0; k < c.size(); k += kPhaseJobs)
+            parts.emplace_back(c.begin() + k, c.begin() + std::min(c.size(), k + kPhaseJobs));
+    }
+    bool shared = false;
+    for (auto &c : parts) {
+        const int nl = std::min<int>(lanes, (int)c.size());
+        int ctas = 0;
+        int rc = stream3d_capacity(plan->streamed[c[0]].g, &ctas);
+        if (rc) return rc;
+        if (ctas < nl) {
+            plan->phases.push_back({0, {c}});
+            continue;
+        }
+        BatchPlan::Phase ph{ctas / nl, std::vector<std::vector<int>>(nl)};
+        std::vector<double> load(nl, 0.0);
+        for (int i : c) {
+            const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            ph.queue[l].push_back(i);
+            load[l] += work(i);
+        }
+        plan->phases.push_back(ph);
+        shared = true;
+    }
+    if (shared) {
+        auto ln = std::make_shared<Lanes>();
+        ST_CUDA(cudaEventCreateWithFlags(&ln->fork, cudaEventDisableTiming));
+        for (int k = 0; k < kLanes - 1; ++k) {
+            ST_CUDA(cudaStreamCreateWithFlags(&ln->s[k], cudaStreamNonBlocking));
+            ST_CUDA(cudaEventCreateWithFlags(&ln->join[k], cudaEventDisableTiming));
+        }
+        plan->lanes = ln;
+    }
+    return STENCIL_OK;
+}
+
+// One whole-GPU job on stream s.
+int run_alone(const StreamedJob &j, cudaStream_t s) {
+    if (!stream_job(j) && j.dims == 3) {
+        // temporally blocked passes leave the result where the pass count
+        // puts it; the batch keeps the ping-pong loop's place (d_u1 for an
+        // even sweep count, d_u2 for an odd one)
+        float *out = nullptr;
+        int rc = run_tb3d(j.g, j.a, j.b, j.iters, j.temporal, s, &out);
+        float *want = (j.iters & 1) ? j.b : j.a;
+        if (!rc && out != want)
+            ST_CUDA(cudaMemcpyAsync(want, out, (size_t)j.g.sz * j.g.nz * sizeof(float),
+                                    cudaMemcpyDeviceToDevice, s));
+        return rc;
+    }
+    if (j.dims == 3) return run_stream3d(j.g, j.a, j.b, j.iters, 0, 0, s, nullptr, 0, true);
+    return tb2d_supported(j.g, 2)
+               ? run_tb2d(j.g, j.a, j.b, j.iters, j.temporal, j.tile_x, j.tile_y, s, nullptr)
+               : run_rows2d(j.g, j.a, j.b, j.iters, s, nullptr);
+}
+
+// The staged jobs' copies in (before the batch's kernels) or out (after).
+int launch_stage(const BatchPlan &plan, const void *ws, bool in, cudaStream_t s) {
+    const StagedJob *t = reinterpret_cast<const StagedJob *>(static_cast<const char *>(ws) + plan.stage_table);
+    const long long rows = plan.staged_rows;
+    const int warps_per_block = kStageThreads / 32;
+    const long long max_warps = (long long)num_sms() * 8 * warps_per_block;
+    const int per_warp = (int)std::max<long long>(1, (rows + max_warps - 1) / max_warps);
+    const long long warps = (rows + per_warp - 1) / per_warp;
+    const int blocks = (int)((warps + warps_per_block - 1) / warps_per_block);
+    k_stage<<<blocks, kStageThreads, 0, s>>>(t, plan.nstaged, rows, per_warp, in);
+    ST_CUDA(cudaGetLastError());
+    return STENCIL_OK;
+}
 
 size_t batch_bytes(int njobs) {
     return ((sizeof(BatchHeader) + 255) & ~(size_t)255) + (size_t)njobs * sizeof(ClusterJob);
@@ -734,9 +949,13 @@ size_t staged_bytes(const stencil_batch_job &b) {
     return (px * rows * sizeof(float) + 255) & ~(size_t)255;
 }
 
-// The job table, then the staged copies (two per ragged job).
+// The job table, the table of staged jobs, then their copies (two per
+// ragged job).
 size_t batch_bytes_for(const stencil_batch_job *jobs, int njobs) {
     size_t n = (batch_bytes(njobs) + 255) & ~(size_t)255;
+    size_t ragged = 0;
+    for (int i = 0; i < njobs; ++i) ragged += staged_bytes(jobs[i]) > 0;
+    n += (ragged * sizeof(StagedJob) + 255) & ~(size_t)255;
     for (int i = 0; i < njobs; ++i) n += 2 * staged_bytes(jobs[i]);
     return n;
 }
@@ -780,8 +999,13 @@ extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, i
     std::vector<ClusterJob> table;
     std::vector<double> work;
     BatchPlan plan;
-    size_t stage_off = (batch_bytes(njobs) + 255) & ~(size_t)255;
+    std::vector<StagedJob> staged;
+    int ragged = 0;
+    for (int i = 0; i < njobs; ++i) ragged += staged_bytes(jobs[i]) > 0;
+    plan.stage_table = (batch_bytes(njobs) + 255) & ~(size_t)255;
+    size_t stage_off = plan.stage_table + (((size_t)ragged * sizeof(StagedJob) + 255) & ~(size_t)255);
     table.reserve(njobs);
+    const long long stream_min3d = env_cells("STENCIL_BATCH_STREAM_MIN_CELLS_3D", kStreamMinCells3d);
     for (int i = 0; i < njobs; ++i) {
         const stencil_batch_job &b = jobs[i];
         stencil_params p;
@@ -813,8 +1037,10 @@ extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, i
             st.nx = b.nx;
             st.px = px;
             st.rows = (long long)b.ny * (b.dims == 3 ? b.nz : 1);
+            st.row0 = plan.staged_rows;
+            plan.staged_rows += st.rows;
             stage_off += 2 * sb;
-            plan.staged.push_back(st);
+            staged.push_back(st);
             ga = st.sa;
             gb = st.sb;
             g.sy = px;
@@ -823,7 +1049,7 @@ extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, i
         ClusterJob j = make_job(g, p.dims, ga, gb, b.iterations, csize, b.temporal);
         // small non-resident 3-D grids stay on clusters, many at a time: a
         // whole-GPU launch of one of them is latency-bound
-        const bool big3d = (long long)cell_count(p) >= kStreamMinCells3d;
+        const bool big3d = (long long)cell_count(p) >= stream_min3d;
         if (!j.resident && ((p.dims == 3 && big3d && stream3d_supported(g)) ||
                             (p.dims == 2 && rows2d_supported(g, 2)))) {
             plan.streamed.push_back({g, ga, gb, b.iterations, p.dims, b.temporal, b.tile_x,
@@ -833,6 +1059,9 @@ extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, i
         table.push_back(j);
         work.push_back((double)cell_count(p) * b.iterations);
     }
+    plan.nstaged = (int)staged.size();
+    int rcg = plan_phases(&plan);
+    if (rcg) return rcg;
     const int nc = (int)table.size();
     // Largest job first: the queue hands them out in this order.
     std::vector<int> order(nc);
@@ -852,6 +1081,9 @@ extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, i
     if (nc)
         ST_CUDA(cudaMemcpyAsync(ws + hb, sorted.data(), nc * sizeof(ClusterJob),
                                 cudaMemcpyHostToDevice, s));
+    if (!staged.empty())
+        ST_CUDA(cudaMemcpyAsync(ws + plan.stage_table, staged.data(),
+                                staged.size() * sizeof(StagedJob), cudaMemcpyHostToDevice, s));
     ST_CUDA(cudaStreamSynchronize(s));
     remember(d_workspace, plan);
     return STENCIL_OK;
@@ -864,11 +1096,9 @@ extern "C" int stencil_batch_launch(const void *d_workspace, stencil_stream_t st
     if (!recall(d_workspace, &plan))
         return fail(STENCIL_EINVAL, "workspace was not prepared by stencil_batch_prepare");
     const BatchHeader &h = plan.h;
-    for (const StagedJob &st : plan.staged) {
-        ST_CUDA(cudaMemcpy2DAsync(st.sa, st.px * sizeof(float), st.ua, st.nx * sizeof(float),
-                                  st.nx * sizeof(float), st.rows, cudaMemcpyDeviceToDevice, s));
-        ST_CUDA(cudaMemcpy2DAsync(st.sb, st.px * sizeof(float), st.ub, st.nx * sizeof(float),
-                                  st.nx * sizeof(float), st.rows, cudaMemcpyDeviceToDevice, s));
+    if (plan.nstaged) {
+        int rc = launch_stage(plan, d_workspace, true, s);
+        if (rc) return rc;
     }
     if (h.njobs) {
         const size_t hb = (sizeof(BatchHeader) + 255) & ~(size_t)255;
@@ -877,32 +1107,38 @@ extern "C" int stencil_batch_launch(const void *d_workspace, stencil_stream_t st
         int rc = launch_cluster_jobs(table, h.njobs, queue, std::min(h.clusters, h.njobs), h.cluster_size, s);
         if (rc) return rc;
     }
-    for (const StreamedJob &j : plan.streamed) {
-        int rc;
-        if (j.dims == 3 && j.temporal >= 2 && !j.g.legacy && j.g.sy == j.g.nx && tb3d_supported(j.g)) {
-            // temporally blocked passes leave the result where the pass count
-            // puts it; the batch keeps the ping-pong loop's place (d_u1 for
-            // an even sweep count, d_u2 for an odd one)
-            float *out = nullptr;
-            rc = run_tb3d(j.g, j.a, j.b, j.iters, j.temporal, s, &out);
-            float *want = (j.iters & 1) ? j.b : j.a;
-            if (!rc && out != want)
-                ST_CUDA(cudaMemcpyAsync(want, out, (size_t)j.g.sz * j.g.nz * sizeof(float),
-                                        cudaMemcpyDeviceToDevice, s));
-        } else if (j.dims == 3) {
-            rc = run_stream3d(j.g, j.a, j.b, j.iters, 0, 0, s, nullptr, 0, true);
-        } else {
-            rc = tb2d_supported(j.g, 2)
-                     ? run_tb2d(j.g, j.a, j.b, j.iters, j.temporal, j.tile_x, j.tile_y, s, nullptr)
-                     : run_rows2d(j.g, j.a, j.b, j.iters, s, nullptr);
+    for (const BatchPlan::Phase &ph : plan.phases) {
+        if (ph.queue.size() == 1) {
+            for (int i : ph.queue[0]) {
+                int rc = run_alone(plan.streamed[i], s);
+                if (rc) return rc;
+            }
+            continue;
+        }
+        // lanes side by side: the first on the caller's stream, the others
+        // on the workspace's streams, forked from and joined back into it
+        const Lanes &ln = *plan.lanes;
+        const int nl = (int)ph.queue.size();
+        ST_CUDA(cudaEventRecord(ln.fork, s));
+        int rc = STENCIL_OK;
+        for (int l = 0; l < nl; ++l) {
+            cudaStream_t sl = l ? ln.s[l - 1] : s;
+            if (l) ST_CUDA(cudaStreamWaitEvent(sl, ln.fork, 0));
+            for (int i : ph.queue[l]) {
+                const StreamedJob &x = plan.streamed[i];
+                if (!rc) rc = run_stream3d(x.g, x.a, x.b, x.iters, 0, 0, sl, nullptr, 0, true, ph.ctas);
+            }
+        }
+        // joined even after a failure, so that a capture stays well formed
+        for (int l = 1; l < nl; ++l) {
+            ST_CUDA(cudaEventRecord(ln.join[l - 1], ln.s[l - 1]));
+            ST_CUDA(cudaStreamWaitEvent(s, ln.join[l - 1], 0));
         }
         if (rc) return rc;
     }
-    for (const StagedJob &st : plan.staged) {
-        ST_CUDA(cudaMemcpy2DAsync(st.ua, st.nx * sizeof(float), st.sa, st.px * sizeof(float),
-                                  st.nx * sizeof(float), st.rows, cudaMemcpyDeviceToDevice, s));
-        ST_CUDA(cudaMemcpy2DAsync(st.ub, st.nx * sizeof(float), st.sb, st.px * sizeof(float),
-                                  st.nx * sizeof(float), st.rows, cudaMemcpyDeviceToDevice, s));
+    if (plan.nstaged) {
+        int rc = launch_stage(plan, d_workspace, false, s);
+        if (rc) return rc;
     }
     return STENCIL_OK;
 }
@@ -914,6 +1150,20 @@ extern "C" int stencil_batch_plan(const void *d_workspace, int *cluster_jobs, in
         return fail(STENCIL_EINVAL, "workspace was not prepared by stencil_batch_prepare");
     *cluster_jobs = plan.h.njobs;
     *whole_gpu_jobs = (int)plan.streamed.size();
+    return STENCIL_OK;
+}
+
+extern "C" int stencil_batch_side_by_side(const void *d_workspace, int *groups, int *jobs) {
+    if (!d_workspace || !groups || !jobs) return fail(STENCIL_EINVAL, "null argument");
+    BatchPlan plan;
+    if (!recall(d_workspace, &plan))
+        return fail(STENCIL_EINVAL, "workspace was not prepared by stencil_batch_prepare");
+    *groups = *jobs = 0;
+    for (const BatchPlan::Phase &ph : plan.phases)
+        if (ph.queue.size() > 1) {
+            ++*groups;
+            for (const auto &q : ph.queue) *jobs += (int)q.size();
+        }
     return STENCIL_OK;
 }
 

@@ -5,24 +5,19 @@
 //     RA = 8 cells, so that every TMA x coordinate of the 2-byte grid is
 //     16-byte aligned -- into a ring of NS shared-memory slots (full/empty
 //     mbarriers, bounded waits);
-//   * a consumer thread owns 4 consecutive cells of one row; every 16-bit
-//     value it reads is widened to FP32 once (exact) and the sums run on
-//     packed FP32 pairs (add.rn.f32x2: two cells per instruction):
-//       - axis i: a sliding window over the 12 cells x-4 .. x+7 of the row
-//         (the first cell's 2R+1-cell window sum, then one add and one
-//         subtraction per further cell, minus the centre);
-//       - axis j: the 2R rows above and below from the centre slot;
-//       - axis k: a running sum over the 2R+1 planes z-R .. z+R kept in a
-//         register queue of widened planes (add the newest plane, subtract
-//         the centre for the output, subtract the oldest before moving on;
-//         restarted at every z-chunk);
-//     its rhs values come from global memory a few planes ahead;
-//   * sum / C + rhs is one fused multiply-add by RN(1/C).
-// The correction equation is not bound to the reference's summation order:
-// these sums differ from an in-order sum only by FP32 roundings, far below
-// the 16-bit storage rounding of every correction sweep.  Per cell update the
-// sweep reads 4 bytes (e and rhs) and writes 2, against 8 for an FP32 sweep;
-// the border band of e_out is never written.
+//   * a consumer thread owns 4 consecutive cells of one row: it converts the
+//     z-neighbours once, when their plane arrives, into an FP32 register queue
+//     of 2R+1 planes; x- and y-neighbours come from the centre slot as 8-byte
+//     loads and enter the FP32 sums through mixed-precision adds
+//     (add.rn.f32.bf16 / .f16: the 16-bit operand is converted exactly, one
+//     rounding, no separate conversion); its rhs values come from global
+//     memory one plane ahead;
+//   * the sum runs in the order of the FP32 sweep (axis i, j, k; offsets -R..-1,
+//     +1..+R) and starts from its first term; sum / C + rhs is one fused
+//     multiply-add by RN(1/C) (within an FP32 ulp of the division, far below
+//     the 16-bit storage rounding).
+// Per cell update it reads 4 bytes (e and rhs) and writes 2, against 8 for an
+// FP32 sweep; the border band of e_out is never written.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -80,23 +75,62 @@ struct Cvt<__half> {
     static constexpr CUtensorMapDataType kTma = CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
 };
 
+// acc + value of cell c (0 .. 11) of the 6 words holding cells x-4 .. x+7
+template <typename E, int CELL>
+__device__ __forceinline__ float add_cell(const uint32_t (&wd)[6], float acc) {
+    return Cvt<E>::template add<CELL & 1>(wd[CELL >> 1], acc);
+}
+
+// the four cells of one 8-byte row segment added to four sums
+template <typename E>
+__device__ __forceinline__ void add_row(uint2 v, float (&acc)[4]) {
+    acc[0] = Cvt<E>::template add<0>(v.x, acc[0]);
+    acc[1] = Cvt<E>::template add<1>(v.x, acc[1]);
+    acc[2] = Cvt<E>::template add<0>(v.y, acc[2]);
+    acc[3] = Cvt<E>::template add<1>(v.y, acc[3]);
+}
+
+template <int E0, int O, int R, typename E>
+__device__ __forceinline__ void add_x(const uint32_t (&wd)[6], float (&acc)[4]) {
+    acc[E0] = add_cell<E, 4 + E0 + O>(wd, acc[E0]);
+}
+
 template <typename E>
 __device__ __forceinline__ float4 to4(uint2 v) {
     const float2 a = Cvt<E>::two(v.x), b = Cvt<E>::two(v.y);
     return make_float4(a.x, a.y, b.x, b.y);
 }
 
-// Packed FP32 pair helpers over the four cells (pairs (0,1) and (2,3)).
-struct Quad {
-    float2 lo, hi;
-};
-__device__ __forceinline__ Quad qadd(Quad a, float4 v) {
-    return {fadd2(a.lo, make_float2(v.x, v.y)), fadd2(a.hi, make_float2(v.z, v.w))};
+// axis-i sum of the four cells in the reference order (offsets -R..-1, +1..+R)
+template <typename E, int R, int O = -R>
+__device__ __forceinline__ void xsum(const uint32_t (&wd)[6], float (&acc)[4]) {
+    if constexpr (O == -R) {
+        acc[0] = add_cell<E, 4 + 0 + O>(wd, -0.0f);
+        acc[1] = add_cell<E, 4 + 1 + O>(wd, -0.0f);
+        acc[2] = add_cell<E, 4 + 2 + O>(wd, -0.0f);
+        acc[3] = add_cell<E, 4 + 3 + O>(wd, -0.0f);
+    } else if constexpr (O != 0) {
+        acc[0] = add_cell<E, 4 + 0 + O>(wd, acc[0]);
+        acc[1] = add_cell<E, 4 + 1 + O>(wd, acc[1]);
+        acc[2] = add_cell<E, 4 + 2 + O>(wd, acc[2]);
+        acc[3] = add_cell<E, 4 + 3 + O>(wd, acc[3]);
+    }
+    if constexpr (O < R) xsum<E, R, O + 1>(wd, acc);
 }
-__device__ __forceinline__ Quad qsub(Quad a, float4 v) {
-    return {fadd2(a.lo, make_float2(-v.x, -v.y)), fadd2(a.hi, make_float2(-v.z, -v.w))};
+
+// four FP32 queue values added to four sums (as pairs where the kernel is
+// issue-bound, R >= 3; the same roundings either way)
+template <bool PK>
+__device__ __forceinline__ void add_q(float4 v, float (&acc)[4]) {
+    if constexpr (PK) {
+        const float2 a = fadd2(make_float2(acc[0], acc[1]), make_float2(v.x, v.y));
+        const float2 b = fadd2(make_float2(acc[2], acc[3]), make_float2(v.z, v.w));
+        acc[0] = a.x; acc[1] = a.y; acc[2] = b.x; acc[3] = b.y;
+    } else {
+        acc[0] += v.x; acc[1] += v.y; acc[2] += v.z; acc[3] += v.w;
+    }
 }
-__device__ __forceinline__ Quad qadd(Quad a, Quad b) { return {fadd2(a.lo, b.lo), fadd2(a.hi, b.hi)}; }
+
 
 constexpr int kTX = 128, kTY = 16, kNS = 16, kRA = 8;
 
@@ -109,9 +143,8 @@ struct LpShape {
     static constexpr int CWARPS = kTY;  // one warp per row, 4 cells per lane
     static constexpr int THREADS = 32 * CWARPS + 32;
     static constexpr int SMEM_BYTES = kNS * SLOT_BYTES + 128 + 2 * kNS * 8;
-    // two CTAs per SM where the registers allow it without spills (R = 1:
-    // 34 warps per SM)
-    static constexpr int MIN_BLOCKS = R <= 1 ? 2 : 1;
+    // two CTAs per SM where the registers allow it (R <= 2: 34 warps per SM)
+    static constexpr int MIN_BLOCKS = R <= 2 ? 2 : 1;
 };
 
 template <typename E, int R>
@@ -124,6 +157,7 @@ __global__ void __launch_bounds__(LpShape<R>::THREADS, LpShape<R>::MIN_BLOCKS)
     constexpr int QN = 2 * R + 1;
     constexpr int PF = R == 4 ? 3 : QN;  // rhs prefetch distance (registers at R = 4)
     static_assert(QN % PF == 0, "the rhs ring must divide the plane queue");
+    constexpr bool PK = R >= 3;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char *ring = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
@@ -169,7 +203,7 @@ __global__ void __launch_bounds__(LpShape<R>::THREADS, LpShape<R>::MIN_BLOCKS)
     // byte offset of this thread's 4 cells in a slot (row cy + R, cell RA + 4 cx)
     const int own = ((cy + R) * S::PW + kRA + 4 * cx) * 2;
     constexpr int ROW = S::PW * 2;
-    uint2 qz[QN];  // the planes of the running sum, as stored (16-bit)
+    float4 qz[QN];
     uint32_t qb = 0;
     for (int item = blockIdx.x; item < items; item += gridDim.x) {
         const int t = item % ntiles, ch = item / ntiles;
@@ -180,17 +214,12 @@ __global__ void __launch_bounds__(LpShape<R>::THREADS, LpShape<R>::MIN_BLOCKS)
         const bool live = x < g.nx && in_range(y, g.ny, R);
         const bool xin = x >= R && x + 3 < g.nx - R;
         const long long rowoff = (long long)y * g.sy + x;
-        // running sum over the queued planes z0-R .. z0+R-1 (axis k); the
-        // queue keeps each plane's four 16-bit values until it leaves the sum
-        Quad fz = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
 #pragma unroll
         for (int p = 0; p < 2 * R; ++p) {
             const uint32_t q = qb + p;
             const int s = q & (kNS - 1);
             if (!mbar_wait_bounded(&full[s], (q / kNS) & 1)) return;
-            qz[p] = *reinterpret_cast<const uint2 *>(ring + s * S::SLOT_BYTES + own);
-            const float4 v = to4<E>(qz[p]);
-            fz = p ? qadd(fz, v) : Quad{make_float2(v.x, v.y), make_float2(v.z, v.w)};
+            qz[p] = to4<E>(*reinterpret_cast<const uint2 *>(ring + s * S::SLOT_BYTES + own));
             if (p < R || p >= np - R) release(s);
         }
         // rhs of planes z .. z+PF-1 in a register ring, each fetched PF plane
@@ -214,48 +243,39 @@ __global__ void __launch_bounds__(LpShape<R>::THREADS, LpShape<R>::MIN_BLOCKS)
                     rq[ph % PF] = __ldg(reinterpret_cast<const uint2 *>(rhs + (long long)(z + PF) * g.sz + rowoff));
                 const int sc = (qb + step + R) & (kNS - 1);
                 const unsigned char *cb = ring + sc * S::SLOT_BYTES + own;
-                // axis i: cells x-4 .. x+7 of row y, widened once; window sums
-                // over x+e-R .. x+e+R slide by one cell, minus the centre
-                float w[12];
+                // cells x-4 .. x+7 of row y as six 2-cell words; x- and y-neighbours
+                // are added straight from the 16-bit values (mixed-precision adds)
+                uint32_t wd[6];
                 {
-                    const float4 a = to4<E>(*reinterpret_cast<const uint2 *>(cb - 8));
-                    const float4 c = to4<E>(*reinterpret_cast<const uint2 *>(cb));
-                    const float4 b = to4<E>(*reinterpret_cast<const uint2 *>(cb + 8));
-                    w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w;
-                    w[4] = c.x; w[5] = c.y; w[6] = c.z; w[7] = c.w;
-                    w[8] = b.x; w[9] = b.y; w[10] = b.z; w[11] = b.w;
+                    const uint2 a = *reinterpret_cast<const uint2 *>(cb - 8);
+                    const uint2 c = *reinterpret_cast<const uint2 *>(cb);
+                    const uint2 b = *reinterpret_cast<const uint2 *>(cb + 8);
+                    wd[0] = a.x; wd[1] = a.y; wd[2] = c.x; wd[3] = c.y; wd[4] = b.x; wd[5] = b.y;
                 }
-                float f0 = w[4 - R];
-#pragma unroll
-                for (int o = -R + 1; o <= R; ++o) f0 += w[4 + o];
-                const float f1 = (f0 - w[4 - R]) + w[5 + R];
-                const float f2 = (f1 - w[5 - R]) + w[6 + R];
-                const float f3 = (f2 - w[6 - R]) + w[7 + R];
-                Quad acc = {fadd2(make_float2(f0, f1), make_float2(-w[4], -w[5])),
-                            fadd2(make_float2(f2, f3), make_float2(-w[6], -w[7]))};
+                float acc[4];
+                // axis i; the first term starts the sum (x + -0 = x exactly)
+                xsum<E, R>(wd, acc);
                 // axis j
 #pragma unroll
                 for (int o = -R; o <= R; ++o) {
                     if (!o) continue;
-                    acc = qadd(acc, to4<E>(*reinterpret_cast<const uint2 *>(cb + o * ROW)));
+                    add_row<E>(*reinterpret_cast<const uint2 *>(cb + o * ROW), acc);
                 }
+                // axis k, planes z-R .. z-1
+#pragma unroll
+                for (int o = -R; o <= -1; ++o) add_q<PK>(qz[(ph + R + o + QN) % QN], acc);
                 release(sc);
-                // axis k: the newest plane z+R joins the running sum, which
-                // then holds planes z-R .. z+R; the centre plane (this row's
-                // own cells, w[4..7]) is excluded
                 {
                     const int pn = step + 2 * R;
                     const uint32_t q = qb + pn;
                     const int s = q & (kNS - 1);
                     if (!mbar_wait_bounded(&full[s], (q / kNS) & 1)) return;
-                    qz[(ph + 2 * R) % QN] = *reinterpret_cast<const uint2 *>(ring + s * S::SLOT_BYTES + own);
+                    qz[(ph + 2 * R) % QN] =
+                        to4<E>(*reinterpret_cast<const uint2 *>(ring + s * S::SLOT_BYTES + own));
                     if (pn >= np - R) release(s);
                 }
-                fz = qadd(fz, to4<E>(qz[(ph + 2 * R) % QN]));
-                acc = qadd(acc, qsub(fz, make_float4(w[4], w[5], w[6], w[7])));
-                // the oldest plane z-R leaves the running sum
-                fz = qsub(fz, to4<E>(qz[ph % QN]));
-                float acc4[4] = {acc.lo.x, acc.lo.y, acc.hi.x, acc.hi.y};
+#pragma unroll
+                for (int o = 1; o <= R; ++o) add_q<PK>(qz[(ph + R + o) % QN], acc);
                 if (live) {
                     // sum / C + rhs as one fused multiply-add by RN(1/C): the
                     // correction is stored in 16 bits, so the division's last
@@ -263,9 +283,16 @@ __global__ void __launch_bounds__(LpShape<R>::THREADS, LpShape<R>::MIN_BLOCKS)
                     float out[4];
                     constexpr float kInv = 1.0f / (float)C;
                     const float2 r01 = Cvt<E>::two(rc.x), r23 = Cvt<E>::two(rc.y);
-                    const float2 a = ffma2(make_float2(acc4[0], acc4[1]), make_float2(kInv, kInv), r01);
-                    const float2 b = ffma2(make_float2(acc4[2], acc4[3]), make_float2(kInv, kInv), r23);
-                    out[0] = a.x; out[1] = a.y; out[2] = b.x; out[3] = b.y;
+                    if constexpr (PK) {
+                        const float2 a = ffma2(make_float2(acc[0], acc[1]), make_float2(kInv, kInv), r01);
+                        const float2 b = ffma2(make_float2(acc[2], acc[3]), make_float2(kInv, kInv), r23);
+                        out[0] = a.x; out[1] = a.y; out[2] = b.x; out[3] = b.y;
+                    } else {
+                        out[0] = fmaf(acc[0], kInv, r01.x);
+                        out[1] = fmaf(acc[1], kInv, r01.y);
+                        out[2] = fmaf(acc[2], kInv, r23.x);
+                        out[3] = fmaf(acc[3], kInv, r23.y);
+                    }
                     E *dst = eo + (long long)z * g.sz + rowoff;
                     if (xin) {
                         uint2 o2;

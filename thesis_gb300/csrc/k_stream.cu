@@ -18,7 +18,7 @@
 //     slot with 16-byte shared loads.  So a slot is needed only while its
 //     plane is the newest or the centre: the ring holds R+1 planes plus the
 //     planes in flight.
-// Out-of-grid box cells arrive as zeros (TMA out-of-bounds fill) and are never
+// Out-of-grid box cells arrive as NaN (TMA out-of-bounds fill) and are never
 // used by an updated cell.  Each input cell is read from HBM once per sweep;
 // halos of neighbouring tiles and chunks are re-read from L2.
 //
@@ -460,8 +460,10 @@ bool stream3d_supported(const Geom &g) {
     return g.sy % 4 == 0 && (g.radius >= 1 && g.radius <= 4);
 }
 
-int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int tile_y,
-                 cudaStream_t s, float **res, int shape_hint, bool persistent) {
+namespace {
+
+// The shape run_stream3d sweeps with (see there).
+int stream_shape(const Geom &g, int tile_x, int tile_y, int shape_hint, bool persistent) {
     const int R = g.radius;
     // Defaults measured fastest at 512^3 on GB300 (a launch per sweep,
     // GCell/s): R <= 2 one row per thread with the 16-slot ring (R = 1: 701
@@ -482,6 +484,26 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     const bool big = (long long)g.nx * g.ny * g.nz >= (1LL << 25);
     if (persistent && !(shape_hint >= 1 && shape_hint <= 6))
         shape = R == 1 ? 3 : (R == 2 ? (big ? 6 : 5) : 4);
+    return shape;
+}
+
+}  // namespace
+
+int stream3d_capacity(const Geom &g, int *ctas) {
+    *ctas = 0;
+    StreamKernel k = pick(g.radius, stream_shape(g, 0, 0, 0, true));
+    if (!k.multi) return fail(STENCIL_EUNSUPPORTED, "no persistent stream kernel for radius %d", g.radius);
+    int per_sm = 0;
+    int rc = kernel_residency(k.multi, k.threads, k.smem, &per_sm);
+    if (rc) return rc;
+    *ctas = per_sm * num_sms();
+    return STENCIL_OK;
+}
+
+int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int tile_y,
+                 cudaStream_t s, float **res, int shape_hint, bool persistent, int max_ctas) {
+    const int R = g.radius;
+    const int shape = stream_shape(g, tile_x, tile_y, shape_hint, persistent);
     StreamKernel k = pick(R, shape);
     if (!k.fn) return fail(STENCIL_EUNSUPPORTED, "stream kernel has no radius-%d instance", R);
     if (persistent && !k.multi)
@@ -492,7 +514,9 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     int rc = kernel_residency(fn, k.threads, k.smem, &per_sm);
     if (rc) return rc;
     if (per_sm < 1) return fail(STENCIL_EUNSUPPORTED, "stream kernel does not fit on an SM");
-    const int resident = per_sm * num_sms();
+    // at most max_ctas CTAs when given (a batch runs two mid-size grids side by
+    // side, each on part of the GPU)
+    const int resident = max_ctas > 0 ? std::min(per_sm * num_sms(), max_ctas) : per_sm * num_sms();
     const int tiles_x = (g.nx + k.tx - 1) / k.tx, tiles_y = (g.ny + k.ty - 1) / k.ty;
     const int tiles = tiles_x * tiles_y;
     const int zin = g.nz - 2 * R;
@@ -523,8 +547,13 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
     CUtensorMap maps[2];
     const long long dims[3] = {g.nx, g.ny, g.nz};
     const int box[3] = {k.tx + 2 * ((R + 3) & ~3), k.ty + 2 * R, 1};
-    rc = make_tensor_map(&maps[0], a, 3, dims, box, g.sy);
-    if (!rc) rc = make_tensor_map(&maps[1], b, 3, dims, box, g.sy);
+    // Box cells outside the grid arrive as NaN: no stored cell reads them,
+    // and the epilogue's range test (fminf / fmaxf) ignores the NaN sums of
+    // the unstored cells past the last column of a width that is not a
+    // multiple of 4 -- zero sums there sent whole warps to the slow division
+    // (160^2 x 161 R = 2: 25.0 us per sweep against 10.8 at 160^3).
+    rc = make_tensor_map(&maps[0], a, 3, dims, box, g.sy, true);
+    if (!rc) rc = make_tensor_map(&maps[1], b, 3, dims, box, g.sy, true);
     if (rc) return rc;
     Geom gg = g;
     int tx_ = tiles_x, ty_ = tiles_y, it_ = items;

@@ -537,9 +537,11 @@ int run_tb2d(const Geom &g, float *a, float *b, int iters, int temporal, int til
         return fail(STENCIL_EUNSUPPORTED, "2-D temporal blocking needs a row pitch %% 4 == 0 and R <= 4");
     const int ctas = tb2_max_ctas(g.radius);
     Tb2Plan p;
-    // a caller tile that does not fit falls back to the library's choice
+    // a caller tile (then a caller depth) that does not fit falls back to the
+    // library's choice
     if (ctas <= 0 || (!choose_plan(g, iters, temporal, tile_x, tile_y, ctas, &p) &&
-                      !choose_plan(g, iters, temporal, 0, 0, ctas, &p)))
+                      !choose_plan(g, iters, temporal, 0, 0, ctas, &p) &&
+                      !choose_plan(g, iters, 0, 0, 0, ctas, &p)))
         return fail(STENCIL_EUNSUPPORTED, "grid too large for one tile per SM");
     if (res) *res = (iters & 1) ? b : a;
     if (iters <= 0) return STENCIL_OK;

@@ -121,6 +121,7 @@ def load() -> ctypes.CDLL:
         "stencil_batch_launch": (i, [vp, vp]),
         "stencil_batch_forget": (i, [vp]),
         "stencil_batch_plan": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(i)]),
+        "stencil_batch_side_by_side": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(i)]),
         "stencil_ir_workspace_bytes": (i, [P, ctypes.POINTER(IrParams), ctypes.POINTER(sz)]),
         "stencil_ir_solve": (i, [P, ctypes.POINTER(IrParams), vp, vp, sz, vp,
                                  ctypes.POINTER(IrResult)]),

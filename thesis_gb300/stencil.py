@@ -285,6 +285,14 @@ class Batch:
                    "stencil_batch_plan")
         return c.value, w.value
 
+    def side_by_side(self):
+        """(sets of lanes that run side by side, each lane a queue of jobs on
+        a share of the GPU; jobs in them)."""
+        g, n = ctypes.c_int(), ctypes.c_int()
+        _lib.check(_lib.load().stencil_batch_side_by_side(self.ws, ctypes.byref(g), ctypes.byref(n)),
+                   "stencil_batch_side_by_side")
+        return g.value, n.value
+
     def kernel_launches(self):
         """Kernel launches of one ``launch`` (one replay of its CUDA graph)."""
         c, w = self.plan()
