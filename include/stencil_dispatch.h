@@ -200,15 +200,16 @@ STENCIL_API int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, 
  * persistent cluster launch over a device work queue (every cluster the
  * device can hold) for the jobs that a cluster sweeps, then, for each job too
  * large for a cluster's shared memory, one persistent launch of its own, and
- * the copies out.  Those launches run on the whole GPU, except that mid-size
- * 3-D jobs (below 2^25 cells) of one radius and mode run in lanes side by
- * side, each lane a queue of jobs on its share of the CTAs the device holds
- * (jobs assigned largest first to the lane with the least work), all lanes
- * but the first on streams that prepare creates for the workspace (forked
- * from and joined back into `stream` by events).  Environment variables read
- * by prepare override the defaults: STENCIL_BATCH_LANES (4; 1 = no lanes),
- * STENCIL_BATCH_LANE_MAX_CELLS (2^25; 0 = no lanes) and
- * STENCIL_BATCH_STREAM_MIN_CELLS_3D (1.2 M: 3-D jobs below it that do not fit
+ * the copies out.  Those launches run on the whole GPU, except that 2-D jobs and
+ * mid-size 3-D jobs (below 2^25 cells) of one radius and mode run in lanes
+ * side by side, each lane a queue of jobs on its share of the CTAs the device
+ * holds (jobs assigned largest first to the lane with the least work; 2-D
+ * ones on the rows kernel), all lanes but the first on streams that prepare
+ * creates for the workspace (forked from and joined back into `stream` by
+ * events).  Environment variables read by prepare override the defaults:
+ * STENCIL_BATCH_LANES and STENCIL_BATCH_LANES_2D (4; 1 = no lanes),
+ * STENCIL_BATCH_LANE_MAX_CELLS (2^25) and STENCIL_BATCH_LANE_MAX_CELLS_2D
+ * (2^30; 0 = no lanes), and STENCIL_BATCH_STREAM_MIN_CELLS_3D (1.2 M: 3-D jobs below it that do not fit
  * a cluster's shared memory are swept by a cluster from L2).  Resets the queue
  * counter first.  Asynchronous; allocates nothing; can be captured into a
  * CUDA graph (the queue reset is a memset node, so every replay runs the

@@ -174,9 +174,10 @@ def test_batch_ragged_sides_match_oracle_and_graph_replay(cuda):
     assert S.device_status() == 0
 
 
-# Mid-size 3-D grids too large for the cluster engine: per radius and mode,
-# lanes side by side (each a queue of jobs on its share of the device's
-# CTAs); the LEGACY job has no other job of its kind and runs alone.
+# Grids too large for the cluster engine: per radius and mode, lanes side by
+# side (each a queue of jobs on its share of the device's CTAs); the LEGACY
+# 3-D job and the 2-D R = 2 job have no other job of their kind and run
+# alone.
 PAIRED = [
     ((120, 120, 120), 1, 9, "jacobi"),
     ((130, 128, 136), 1, 8, "jacobi"),
@@ -187,14 +188,18 @@ PAIRED = [
     ((124, 120, 107), 2, 3, "jacobi"),      # ragged
     ((100, 128, 120), 2, 4, "jacobi"),
     ((128, 128, 128), 1, 4, "legacy"),
+    ((800, 804), 1, 9, "jacobi"),           # 2-D: lanes of the rows kernel
+    ((760, 803), 1, 6, "jacobi"),           # ragged
+    ((900, 640), 2, 5, "jacobi"),           # alone (no other 2-D R = 2 job)
 ]
 
 # (STENCIL_BATCH_LANES, STENCIL_BATCH_LANE_MAX_CELLS, expected (lane sets, jobs in them))
-LANES = [("", "", (2, 8)),        # the defaults: 4 lanes below 2^25 cells
-         ("2", "", (2, 8)),       # two lanes, queues of 2 and 1 (R = 1) and 3 and 2 (R = 2)
-         ("8", "", (2, 8)),       # as many lanes as jobs
-         ("1", "", (0, 0)),       # every job alone
-         ("", "0", (0, 0))]
+# (the 2-D lanes keep their defaults: one set of two R = 1 jobs)
+LANES = [("", "", (3, 10)),       # the defaults: 4 lanes below 2^25 cells
+         ("2", "", (3, 10)),      # two lanes, queues of 2 and 1 (R = 1) and 3 and 2 (R = 2)
+         ("8", "", (3, 10)),      # as many lanes as jobs
+         ("1", "", (1, 2)),       # every 3-D job alone
+         ("", "0", (1, 2))]
 
 
 @pytest.mark.parametrize("lanes,cap,expect", LANES)

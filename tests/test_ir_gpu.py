@@ -9,7 +9,10 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("storage,bound", [("bf16", 1e-3), ("fp16", 1.5e-4)])
-@pytest.mark.parametrize("shape,radius,sweeps", [((64, 64, 64), 4, 200), ((48, 56, 64), 2, 150),
+# R = 4 runs the tensor-core correction sweep: partial tiles in x (nx = 136,
+# 64) and y (ny = 72, 33), several z chunks (nz = 100)
+@pytest.mark.parametrize("shape,radius,sweeps", [((64, 64, 64), 4, 200), ((40, 72, 136), 4, 120),
+                                                 ((100, 33, 64), 4, 90), ((48, 56, 64), 2, 150),
                                                  ((256, 256), 1, 400)])
 def test_ir_matches_fp32_and_fp64(cuda, storage, bound, shape, radius, sweeps):
     import torch

@@ -77,8 +77,12 @@ int run_tb2d(const Geom &g, float *a, float *b, int iters, int temporal, int til
 void tb2d_release();
 // Larger 2-D grids: all sweeps in one cooperative launch, a grid-wide barrier
 // between sweeps, register-queue columns (k_rows2d.cu).
+// max_ctas > 0 caps the CTAs of the launch; rows2d_capacity = the CTAs of the
+// device that the kernel for g's radius can hold at once.
 bool rows2d_supported(const Geom &g, int dims);
-int run_rows2d(const Geom &g, float *a, float *b, int iters, cudaStream_t s, float **res);
+int rows2d_capacity(const Geom &g);
+int run_rows2d(const Geom &g, float *a, float *b, int iters, cudaStream_t s, float **res,
+               int max_ctas = 0);
 // All sweeps of one grid on one thread-block cluster (k_cluster.cu).
 int run_cluster(const Geom &g, int dims, float *a, float *b, int iters, cudaStream_t s,
                 float **res);

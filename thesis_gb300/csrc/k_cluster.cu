@@ -800,13 +800,26 @@ constexpr long long kStreamMinCells3d = STENCIL_STREAM_MIN_CELLS_3D;
 
 // 3-D whole-GPU jobs below STENCIL_BATCH_LANE_MAX_CELLS cells (2^25, about
 // 320^3) run side by side in STENCIL_BATCH_LANES lanes, each on that share of
-// the device's CTAs; environment variables of the same names override them
-// at prepare time (lanes 1 or cells 0 = never).
+// the device's CTAs, and 2-D ones below STENCIL_BATCH_LANE_MAX_CELLS_2D (2^30)
+// in STENCIL_BATCH_LANES_2D lanes on the rows kernel; environment variables of
+// the same names override them at prepare time (lanes 1 or cells 0 = never).
+// GB300, the 512-grid benchmark batch: its 56 3-D whole-GPU jobs (R = 2,
+// 106-256^3) 1.93 s alone, 1.64 s in 4 or 8 lanes; its 122 2-D ones
+// (640-2048^2, R = 1) 1.14 s alone (the temporally blocked engine where the
+// grid fits one tile per SM, else the rows kernel), 0.89 / 0.70 / 0.71 s in
+// 2 / 4 / 8 lanes of the rows kernel (8 equal 1000^2 grids: 296 GCell/s alone,
+// 559 in 4 lanes; 2048^2: 577 alone, 630 in 4 lanes, 711 in 2).
 #ifndef STENCIL_BATCH_LANE_MAX_CELLS
 #define STENCIL_BATCH_LANE_MAX_CELLS 33554432
 #endif
 #ifndef STENCIL_BATCH_LANES
 #define STENCIL_BATCH_LANES 4
+#endif
+#ifndef STENCIL_BATCH_LANE_MAX_CELLS_2D
+#define STENCIL_BATCH_LANE_MAX_CELLS_2D 1073741824
+#endif
+#ifndef STENCIL_BATCH_LANES_2D
+#define STENCIL_BATCH_LANES_2D 4
 #endif
 
 long long env_cells(const char *name, long long dflt) {
@@ -833,23 +846,32 @@ long long job_cells(const StreamedJob &j) { return (long long)j.g.nx * j.g.ny * 
 // lane with the least work so far, largest first (longest-processing-time
 // scheduling; work = cells x sweeps).
 int plan_phases(BatchPlan *plan) {
+    auto lanes_env = [](const char *name, long long dflt) {
+        return (int)std::min<long long>(kLanes, std::max<long long>(1, env_cells(name, dflt)));
+    };
     const long long cap = env_cells("STENCIL_BATCH_LANE_MAX_CELLS", STENCIL_BATCH_LANE_MAX_CELLS);
-    const int lanes = (int)std::min<long long>(kLanes, std::max<long long>(
-        1, env_cells("STENCIL_BATCH_LANES", STENCIL_BATCH_LANES)));
+    const long long cap2 = env_cells("STENCIL_BATCH_LANE_MAX_CELLS_2D", STENCIL_BATCH_LANE_MAX_CELLS_2D);
+    const int lanes = lanes_env("STENCIL_BATCH_LANES", STENCIL_BATCH_LANES);
+    const int lanes2 = lanes_env("STENCIL_BATCH_LANES_2D", STENCIL_BATCH_LANES_2D);
     const int n = (int)plan->streamed.size();
     auto work = [&](int i) { return (double)job_cells(plan->streamed[i]) * plan->streamed[i].iters; };
     auto laned = [&](int i) {
         const StreamedJob &j = plan->streamed[i];
+        // a 2-D job with tuning hints runs alone on the engine they tune
+        if (j.dims == 2)
+            return lanes2 > 1 && job_cells(j) < cap2 && !j.temporal && !j.tile_x && !j.tile_y;
         return lanes > 1 && stream_job(j) && job_cells(j) < cap;
     };
-    // kernel class of a laned job
+    // kernel class of a laned job: 3-D by radius, arithmetic and shape
+    // class, 2-D (the rows kernel) by radius
     auto kclass = [&](int i) {
         const StreamedJob &j = plan->streamed[i];
+        if (j.dims == 2) return 20 + j.g.radius;
         return j.g.radius * 4 + (j.g.legacy ? 2 : 0) + (job_cells(j) >= (1LL << 25) ? 1 : 0);
     };
     plan->phases.clear();
     BatchPlan::Phase alone{0, {{}}};
-    std::vector<std::vector<int>> byclass(4 * 5);
+    std::vector<std::vector<int>> byclass(25);
     for (int i = 0; i < n; ++i) {
         if (laned(i)) byclass[kclass(i)].push_back(i);
         else alone.queue[0].push_back(i);
@@ -873,10 +895,15 @@ int plan_phases(BatchPlan *plan) {
     }
     bool shared = false;
     for (auto &c : parts) {
-        const int nl = std::min<int>(lanes, (int)c.size());
+        const StreamedJob &j0 = plan->streamed[c[0]];
+        const int nl = std::min<int>(j0.dims == 2 ? lanes2 : lanes, (int)c.size());
         int ctas = 0;
-        int rc = stream3d_capacity(plan->streamed[c[0]].g, &ctas);
-        if (rc) return rc;
+        if (j0.dims == 2) {
+            ctas = rows2d_capacity(j0.g);
+        } else {
+            int rc = stream3d_capacity(j0.g, &ctas);
+            if (rc) return rc;
+        }
         if (ctas < nl) {
             plan->phases.push_back({0, {c}});
             continue;
@@ -1126,7 +1153,9 @@ extern "C" int stencil_batch_launch(const void *d_workspace, stencil_stream_t st
             if (l) ST_CUDA(cudaStreamWaitEvent(sl, ln.fork, 0));
             for (int i : ph.queue[l]) {
                 const StreamedJob &x = plan.streamed[i];
-                if (!rc) rc = run_stream3d(x.g, x.a, x.b, x.iters, 0, 0, sl, nullptr, 0, true, ph.ctas);
+                if (!rc)
+                    rc = x.dims == 2 ? run_rows2d(x.g, x.a, x.b, x.iters, sl, nullptr, ph.ctas)
+                                     : run_stream3d(x.g, x.a, x.b, x.iters, 0, 0, sl, nullptr, 0, true, ph.ctas);
             }
         }
         // joined even after a failure, so that a capture stays well formed

@@ -159,12 +159,15 @@ bool rows2d_supported(const Geom &g, int dims) {
            (long long)(g.sy / 4) * (g.ny - 2 * g.radius) < (1LL << 31) && rows_ctas(g.radius) > 0;
 }
 
-int run_rows2d(const Geom &g, float *a, float *b, int iters, cudaStream_t s, float **res) {
+int rows2d_capacity(const Geom &g) { return rows_ctas(g.radius); }
+
+int run_rows2d(const Geom &g, float *a, float *b, int iters, cudaStream_t s, float **res,
+               int max_ctas) {
     if (!rows2d_supported(g, 2))
         return fail(STENCIL_EUNSUPPORTED, "persistent 2-D rows kernel: row pitch %% 4 == 0, R <= 4");
     if (res) *res = (iters & 1) ? b : a;
     if (iters <= 0) return STENCIL_OK;
-    const int ctas = rows_ctas(g.radius);
+    const int ctas = max_ctas > 0 ? std::min(max_ctas, rows_ctas(g.radius)) : rows_ctas(g.radius);
     const int nch = (int)(g.sy / 4), rows = g.ny - 2 * g.radius;
     // Row blocks as tall as keeps about four items per resident thread (a
     // taller block re-reads fewer halo rows), at most 64 rows and at least 4

@@ -294,9 +294,12 @@ class Batch:
         return g.value, n.value
 
     def kernel_launches(self):
-        """Kernel launches of one ``launch`` (one replay of its CUDA graph)."""
+        """Kernel launches of one ``launch`` (one replay of its CUDA graph):
+        the cluster launch, one per whole-GPU job, and the two copy kernels
+        of jobs whose nx is not a multiple of 4."""
         c, w = self.plan()
-        return (1 if c else 0) + w
+        ragged = any(u1.shape[-1] % 4 for u1, *_ in self.jobs)
+        return (1 if c else 0) + w + (2 if ragged else 0)
 
     def result(self, k):
         u1, u2, _, iters, _ = self.jobs[k]
