@@ -188,6 +188,7 @@ __global__ void __launch_bounds__(LpShape<R>::THREADS, LpShape<R>::MIN_BLOCKS)
                 const int s = q & (kNS - 1);
                 const uint32_t use = q / kNS;
                 if (use > 0 && !mbar_wait_bounded(&empty[s], (use - 1) & 1)) return;
+                fence_proxy_async();  // the consumers' reads of the slot before the TMA write
                 mbar_arrive_expect_tx(&full[s], S::PLANE_BYTES);
                 tma_load_3d(ring + s * S::SLOT_BYTES, &e_map, &full[s], x0 - kRA, y0 - R,
                             z0 - R + p);
@@ -329,28 +330,26 @@ __global__ void __launch_bounds__(LpShape<R>::THREADS, LpShape<R>::MIN_BLOCKS)
 // of the 2R+1 planes z-R .. z+R (one plane added, one subtracted per step)
 // that also holds the centre, which the -1 of Bx cancels; W is the
 // accumulator the products are added to.  A warp owns one 16 x 16 block of
-// the CTA's 128 x 16 tile, so a cell costs about 0.3 warp instructions
-// against about 1.4 for the per-term mixed-precision adds.  The result
-// differs from the in-order FP32 sum by FP32 roundings only (the correction
-// equation is not bound to the reference's order).
+// the CTA's 128 x 32 tile (16 consumer warps, two 16-row blocks sharing one
+// halo), so a cell costs about 0.3 warp instructions against about 1.4 for
+// the per-term mixed-precision adds.  The result differs from the in-order
+// FP32 sum by FP32 roundings only (the correction equation is not bound to
+// the reference's order).
+//
+// Measured on GB300 (504^3 R = 4, one sweep): per-term adds 240 us; this
+// structure with 128 x 16 tiles and per-thread rhs loads / stores 248 us (9
+// warps per SM: latency-bound); 128 x 32 tiles 195 us (the L1/TEX pipe 90 %
+// busy: per-thread global accesses in the mma fragment layout touch 8
+// half-used sectors per warp instruction); rhs and output by TMA as below:
+// 768^3 refinement 1.24x the FP32 loop.  The producer issues
+// fence.proxy.async after acquiring a slot and before its TMA write into it,
+// ordering the consumers' generic-proxy reads (released to it through the
+// empty mbarrier) before the async-proxy write; repeated runs are
+// bit-identical.  (An earlier form that read rhs and stored its output with
+// per-thread global accesses showed rare differing cells between repeated
+// runs without such a fence.)
 constexpr int kTcTX = 128;
 constexpr int kTcPW = 152;  // slot row: 76 words, so ldmatrix rows hit distinct banks
-
-// RB row blocks of 16 cells per CTA: tile 128 x 16*RB, 8*RB consumer warps,
-// a ring of NS plane slots (at least 2R + 2 = 10: the planes z-R-1 .. z+R of
-// the running sum stay resident, and the rest are loads in flight)
-template <int RB, int NS>
-struct LpTcShape {
-    static constexpr int R = 4;
-    static constexpr int TY = 16 * RB;
-    static constexpr int PH = TY + 2 * R;  // the last block's y product reads rows 16(RB-1) .. +23
-    static constexpr int PLANE_BYTES = kTcPW * PH * 2;
-    static constexpr int SLOT_BYTES = (PLANE_BYTES + 127) & ~127;
-    static constexpr int CWARPS = 8 * RB;
-    static constexpr int THREADS = 32 * CWARPS + 32;
-    static constexpr int SMEM_BYTES = NS * SLOT_BYTES + 128 + 2 * NS * 8;
-    static_assert(NS >= 2 * R + 2, "ring too short for the running z sum");
-};
 
 template <typename E>
 struct Bits;
@@ -441,268 +440,7 @@ __device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity) {
     return __all_sync(0xffffffffu, mbar_wait_bounded(bar, parity));
 }
 
-template <typename E, int RB, int NS, bool PFENCE, bool LATE>
-__global__ void __launch_bounds__(LpTcShape<RB, NS>::THREADS, 1)
-    k_lp_stream_tc(const __grid_constant__ CUtensorMap e_map, E *__restrict__ eo,
-                   const E *__restrict__ rhs, Geom g, int tiles_x, int tiles_y, int zchunk,
-                   int items) {
-    using S = LpTcShape<RB, NS>;
-    constexpr int R = S::R;
-    constexpr int C = 6 * R;
-    constexpr int PF = 4;  // rhs prefetch distance in planes (steps unrolled by PF)
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    unsigned char *ring = reinterpret_cast<unsigned char *>(
-        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
-    uint64_t *full = reinterpret_cast<uint64_t *>(ring + NS * S::SLOT_BYTES);
-    uint64_t *empty = full + NS;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    if (tid == 0) {
-        prefetch_tensormap(&e_map);
-        for (int s = 0; s < NS; ++s) {
-            mbar_init(&full[s], 1);
-            mbar_init(&empty[s], S::CWARPS);
-        }
-        fence_mbar_init();
-    }
-    __syncthreads();
-    const int ntiles = tiles_x * tiles_y;
-
-    if (warp == S::CWARPS) {
-        if (lane != 0) return;
-        uint32_t q = 0;
-        for (int item = blockIdx.x; item < items; item += gridDim.x) {
-            const int t = item % ntiles, ch = item / ntiles;
-            const int x0 = (t % tiles_x) * kTcTX, y0 = (t / tiles_x) * S::TY;
-            const int z0 = R + ch * zchunk, z1 = min(z0 + zchunk, g.nz - R);
-            const int np = (z1 - z0) + 2 * R;
-            for (int p = 0; p < np; ++p, ++q) {
-                const int s = (int)(q % NS);
-                const uint32_t use = q / NS;
-                if (use > 0 && !mbar_wait_bounded(&empty[s], (use - 1) & 1)) return;
-                mbar_arrive_expect_tx(&full[s], S::PLANE_BYTES);
-                tma_load_3d(ring + s * S::SLOT_BYTES, &e_map, &full[s], x0 - 8, y0 - R, z0 - R + p);
-            }
-        }
-        return;
-    }
-
-    const int gq = lane >> 2, tq = lane & 3;  // fragment row group and column pair
-    // constant operands: Bx[window][n block] (b0, b1), Ay16, Ay8
-    uint32_t bx[2][2][2];
-#pragma unroll
-    for (int w = 0; w < 2; ++w)
-#pragma unroll
-        for (int nb = 0; nb < 2; ++nb)
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int k = 2 * tq + 8 * h, n = gq + 8 * nb;
-                const int d0 = (w == 0 ? k - 8 : k + 8) - n;
-                bx[w][nb][h] = coef_bits<E>(xcoef(d0)) | (coef_bits<E>(xcoef(d0 + 1)) << 16);
-            }
-    uint32_t ay16[4], ay8[2];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int m = gq + 8 * (i & 1), k = 2 * tq + 8 * (i >> 1);
-        ay16[i] = coef_bits<E>(ycoef(k, m)) | (coef_bits<E>(ycoef(k + 1, m)) << 16);
-    }
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-        const int m = gq + 8 * i, k = 16 + 2 * tq;
-        ay8[i] = coef_bits<E>(ycoef(k, m)) | (coef_bits<E>(ycoef(k + 1, m)) << 16);
-    }
-    // the warp's 16 x 16 block: tile rows 16 rb .., columns 16 cb .. (slot row
-    // 0 = y0 - 4, slot column 0 = x0 - 8)
-    const int rb = warp >> 3, cw = 16 * (warp & 7), ry = 16 * rb;
-    const int mi = lane >> 3, rr = lane & 7;
-    const uint32_t off_a = ((R + ry + rr + (mi & 1) * 8) * kTcPW + cw + (mi >> 1) * 8) * 2;  // +32: window 2
-    const uint32_t off_b16 = ((ry + rr + (mi & 1) * 8) * kTcPW + cw + 8 + (mi >> 1) * 8) * 2;
-    const uint32_t off_b8 = ((ry + 16 + rr) * kTcPW + cw + 8 + (mi & 1) * 8) * 2;
-    const uint32_t off_w = ((R + ry + gq) * kTcPW + cw + 8 + 2 * tq) * 2;  // +16: n block 1; +HALF: rows +8
-    constexpr uint32_t HALF = 8 * kTcPW * 2;
-    const uint32_t ring_s = smem_u32(ring);
-    auto release = [&](int s) {
-        if constexpr (PFENCE) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[s]);
-    };
-    auto slot_of = [&](uint32_t q) { return (int)(q % NS); };
-    // the thread's four words of a plane slot: [half][n block]
-    auto words = [&](int s, uint32_t (&wv)[2][2]) {
-        const unsigned char *b = ring + s * S::SLOT_BYTES + off_w;
-        wv[0][0] = *reinterpret_cast<const uint32_t *>(b);
-        wv[0][1] = *reinterpret_cast<const uint32_t *>(b + 16);
-        wv[1][0] = *reinterpret_cast<const uint32_t *>(b + HALF);
-        wv[1][1] = *reinterpret_cast<const uint32_t *>(b + HALF + 16);
-    };
-    uint32_t qb = 0;
-    for (int item = blockIdx.x; item < items; item += gridDim.x) {
-        const int t = item % ntiles, ch = item / ntiles;
-        const int x0 = (t % tiles_x) * kTcTX, y0 = (t / tiles_x) * S::TY;
-        const int z0 = R + ch * zchunk, z1 = min(z0 + zchunk, g.nz - R);
-        const int np = (z1 - z0) + 2 * R;
-        // the thread's four cell pairs: rows y0+ry+gq (+8), columns x0+cw+2tq (+8)
-        const int xa = x0 + cw + 2 * tq, ya = y0 + ry + gq;
-        const bool r0 = in_range(ya, g.ny, R), r1 = in_range(ya + 8, g.ny, R);
-        const bool c0 = xa >= R && xa + 1 < g.nx - R, c1 = xa + 8 >= R && xa + 9 < g.nx - R;
-        const bool ok[2][2] = {{r0 && c0, r0 && c1}, {r1 && c0, r1 && c1}};
-        const long long base = (long long)ya * g.sy + xa;  // + h*8*sy + nb*8
-        const long long rowstep = 8 * g.sy;
-        // W = sum of planes 0 .. 2R (z0-R .. z0+R)
-        float2 wsum[2][2];
-#pragma unroll
-        for (int p = 0; p <= 2 * R; ++p) {
-            const uint32_t q = qb + p;
-            if (!warp_wait(&full[slot_of(q)], (q / NS) & 1)) return;
-            uint32_t wv[2][2];
-            words(slot_of(q), wv);
-#pragma unroll
-            for (int h = 0; h < 2; ++h)
-#pragma unroll
-                for (int nb = 0; nb < 2; ++nb) {
-                    const float2 v = Cvt<E>::two(wv[h][nb]);
-                    wsum[h][nb] = p == 0 ? v : fadd2(wsum[h][nb], v);
-                }
-        }
-        // rhs of planes z0 .. z0+PF-1, each fetched PF steps before its use
-        const E *rp = rhs + (long long)z0 * g.sz + base;
-        E *op = eo + (long long)z0 * g.sz + base;
-        uint32_t rq[PF][2][2];
-#pragma unroll
-        for (int p = 0; p < PF; ++p)
-#pragma unroll
-            for (int h = 0; h < 2; ++h)
-#pragma unroll
-                for (int nb = 0; nb < 2; ++nb)
-                    rq[p][h][nb] = (ok[h][nb] && z0 + p < z1)
-                                       ? __ldg(reinterpret_cast<const unsigned *>(rp + p * g.sz + h * rowstep + nb * 8))
-                                       : 0u;
-        rp += PF * g.sz;
-        for (int zb = z0; zb < z1; zb += PF) {
-#pragma unroll
-            for (int ph = 0; ph < PF; ++ph) {
-                const int z = zb + ph;
-                if (z >= z1) break;
-                const int step = z - z0;
-                float wc[2][4];  // W of plane z as the products' C operand
-                int old_slot = -1;
-                if (step > 0) {
-                    // W(z) = W(z-1) + plane z+R - plane z-1-R
-                    const uint32_t qn = qb + step + 2 * R, qo = qb + step - 1;
-                    if (!warp_wait(&full[slot_of(qn)], (qn / NS) & 1)) return;
-                    uint32_t wn[2][2], wo[2][2];
-                    words(slot_of(qn), wn);
-                    words(slot_of(qo), wo);
-#pragma unroll
-                    for (int h = 0; h < 2; ++h)
-#pragma unroll
-                        for (int nb = 0; nb < 2; ++nb) {
-                            const float2 d = ffma2(Cvt<E>::two(wo[h][nb]), make_float2(-1.0f, -1.0f),
-                                                   Cvt<E>::two(wn[h][nb]));
-                            wsum[h][nb] = fadd2(wsum[h][nb], d);
-                        }
-                    old_slot = slot_of(qo);
-                    if constexpr (!LATE) release(old_slot);
-                }
-#pragma unroll
-                for (int nb = 0; nb < 2; ++nb) {
-                    wc[nb][0] = wsum[0][nb].x; wc[nb][1] = wsum[0][nb].y;
-                    wc[nb][2] = wsum[1][nb].x; wc[nb][3] = wsum[1][nb].y;
-                }
-                // centre plane z: the x and y products
-                const uint32_t cs = ring_s + slot_of(qb + step + R) * S::SLOT_BYTES;
-                uint32_t a1[4], a2[4], b16[4], b8[2];
-                ldsm_x4(a1, cs + off_a);
-                ldsm_x4(a2, cs + off_a + 32);
-                ldsm_x4_t(b16, cs + off_b16);
-                ldsm_x2_t(b8, cs + off_b8);
-                float acc[2][4];
-#pragma unroll
-                for (int nb = 0; nb < 2; ++nb) {
-                    float t1[4], t2[4], t3[4];
-                    Mma<E>::k16(t1, a1, bx[0][nb][0], bx[0][nb][1], wc[nb]);
-                    Mma<E>::k16(t2, a2, bx[1][nb][0], bx[1][nb][1], t1);
-                    Mma<E>::k16(t3, ay16, b16[2 * nb], b16[2 * nb + 1], t2);
-                    Mma<E>::k8(acc[nb], ay8, b8[nb], t3);
-                }
-                // sum / C + rhs, stored in 16 bits (pairs of cells)
-                constexpr float kInv = 1.0f / (float)C;
-#pragma unroll
-                for (int h = 0; h < 2; ++h)
-#pragma unroll
-                    for (int nb = 0; nb < 2; ++nb) {
-                        const float2 r = Cvt<E>::two(rq[ph][h][nb]);
-                        const float2 o = ffma2(make_float2(acc[nb][2 * h], acc[nb][2 * h + 1]),
-                                               make_float2(kInv, kInv), r);
-                        if (ok[h][nb])
-                            *reinterpret_cast<uint32_t *>(op + h * rowstep + nb * 8) = Cvt<E>::pack(o.x, o.y);
-                        rq[ph][h][nb] = (ok[h][nb] && z + PF < z1)
-                                            ? __ldg(reinterpret_cast<const unsigned *>(rp + h * rowstep + nb * 8))
-                                            : 0u;
-                    }
-                op += g.sz;
-                rp += g.sz;
-                // the old plane's slot, after this step's stores (its reads
-                // finished long before the fence)
-                if constexpr (LATE)
-                    if (old_slot >= 0) release(old_slot);
-            }
-        }
-        // planes still held: L .. np-1 (L = the last step)
-        const int last = (z1 - z0) - 1;
-        for (int p = last; p < np; ++p) release(slot_of(qb + p));
-        qb += np;
-    }
-}
-
-template <typename E, int RB, int NS, bool PFENCE, bool LATE>
-int run_lp_tc(const Geom &g, const E *e, E *eo, const E *rhs, cudaStream_t s) {
-    using S = LpTcShape<RB, NS>;
-    const void *fn = reinterpret_cast<const void *>(k_lp_stream_tc<E, RB, NS, PFENCE, LATE>);
-    static int per_sm_cached[64] = {0};
-    const int dev = current_device();
-    int per_sm = (dev >= 0 && dev < 64) ? per_sm_cached[dev] : 0;
-    if (!per_sm) {
-        ST_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM_BYTES));
-        ST_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                     cudaSharedmemCarveoutMaxShared));
-        ST_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, S::THREADS, S::SMEM_BYTES));
-        if (per_sm < 1) return fail(STENCIL_EUNSUPPORTED, "tensor-core correction sweep does not fit");
-        if (dev >= 0 && dev < 64) per_sm_cached[dev] = per_sm;
-    }
-    const int resident = per_sm * num_sms();
-    const int tiles_x = (g.nx + kTcTX - 1) / kTcTX, tiles_y = (g.ny + S::TY - 1) / S::TY;
-    const int tiles = tiles_x * tiles_y;
-    const int zin = g.nz - 2 * S::R;
-    int nchunks = 1;
-    double best = 1e30;
-    for (int n = 1; n <= std::max(1, zin / 8); ++n) {
-        const int zc = (zin + n - 1) / n;
-        const long long it = (long long)tiles * ((zin + zc - 1) / zc);
-        const double waves = std::ceil((double)it / resident);
-        const double fill = (double)it / (waves * resident);
-        const double cost = (1.0 + 0.25 * (2.0 * S::R + 1) / zc) / fill + 0.002 * waves;
-        if (cost < best - 1e-9) { best = cost; nchunks = n; }
-    }
-    int zchunk = (zin + nchunks - 1) / nchunks;
-    nchunks = (zin + zchunk - 1) / zchunk;
-    int items = tiles * nchunks;
-    const int grid = std::min(items, resident);
-    CUtensorMap map;
-    const long long dims[3] = {g.nx, g.ny, g.nz};
-    const int box[3] = {kTcPW, S::PH, 1};
-    int rc = make_tensor_map_typed(&map, e, 3, dims, box, Cvt<E>::kTma, 2);
-    if (rc) return rc;
-    Geom gg = g;
-    int tx_ = tiles_x, ty_ = tiles_y;
-    void *args[] = {&map, &eo, &rhs, &gg, &tx_, &ty_, &zchunk, &items};
-    ST_CUDA(cudaLaunchKernel(fn, dim3(grid), dim3(S::THREADS), args, S::SMEM_BYTES, s));
-    return STENCIL_OK;
-}
-
-// The same sweep with its rhs and output moved by TMA instead of per-thread
-// global accesses in the mma fragment layout (8 half-used sectors per warp
-// access; with them the L1/TEX pipe was the limit, 90 % busy at 195 us for
-// 504^3 R = 4):
+// Data movement: the e plane tiles (152 x 40) by TMA into a ring of NE slots;
 //   * the producer also streams each step's rhs tile (136 x 32: 68-word rows,
 //     conflict-free fragment reads) into a ring of 4 slots, issued with the
 //     e plane that the same step first needs;
@@ -791,6 +529,9 @@ __global__ void __launch_bounds__(LpTc3Shape<NE>::THREADS, 1)
                 const int s = (int)(q % NE);
                 const uint32_t use = q / NE;
                 if (use > 0 && !mbar_wait_bounded(&empty[s], (use - 1) & 1)) return;
+                // the consumers' reads of the slot (they arrived after them)
+                // before this TMA write into it
+                fence_proxy_async();
                 mbar_arrive_expect_tx(&full[s], S::E_BYTES);
                 tma_load_3d(ering + s * S::E_SLOT, &e_map, &full[s], x0 - 8, y0 - R, z0 - R + p);
                 if (p >= 2 * R) {
@@ -798,6 +539,7 @@ __global__ void __launch_bounds__(LpTc3Shape<NE>::THREADS, 1)
                     const int rs = (int)(qr % NR);
                     const uint32_t ruse = qr / NR;
                     if (ruse > 0 && !mbar_wait_bounded(&rempty[rs], (ruse - 1) & 1)) return;
+                    fence_proxy_async();
                     mbar_arrive_expect_tx(&rfull[rs], S::R_BYTES);
                     tma_load_3d(rring + rs * S::R_SLOT, &r_map, &rfull[rs], x0, y0, z0 + p - 2 * R);
                     ++qr;
@@ -841,10 +583,8 @@ __global__ void __launch_bounds__(LpTc3Shape<NE>::THREADS, 1)
     constexpr uint32_t HALF = 8 * kTcPW * 2, RHALF = 8 * S::RW * 2, OHALF = 8 * 16 * 2;
     const uint32_t ering_s = smem_u32(ering);
     unsigned char *stage0 = ostage + warp * 2 * S::STAGE;
-    // a slot's reads are done: order them before the producer's next TMA
-    // write into it, then one arrival per warp
+    // a slot's reads are done: one arrival per warp
     auto release = [&](uint64_t *bar) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncwarp();
         if (lane == 0) mbar_arrive(bar);
     };
@@ -952,7 +692,7 @@ __global__ void __launch_bounds__(LpTc3Shape<NE>::THREADS, 1)
                 }
             // the staged block becomes visible to the bulk copy, then one lane
             // stores it
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            fence_proxy_async();
             __syncwarp();
             if (lane == 0) {
                 tma_store_3d(&o_map, st, x0 + cw, y0 + ry, z);
@@ -1017,15 +757,14 @@ int run_lp_tc3(const Geom &g, const E *e, E *eo, const E *rhs, cudaStream_t s) {
     return STENCIL_OK;
 }
 
-// The R = 4 correction sweep: on the tensor cores with 128 x 32 tiles (2),
-// 128 x 16 tiles (1), or with per-term mixed-precision adds (0), as the
-// environment variable STENCIL_LP_MMA says (default 2).
-int lp_mma_mode() {
-    static const int mode = [] {
+// The R = 4 correction sweep on the tensor cores unless the environment
+// variable STENCIL_LP_MMA is 0 (then with the per-term mixed-precision adds).
+bool lp_mma_enabled() {
+    static const bool on = [] {
         const char *v = std::getenv("STENCIL_LP_MMA");
-        return (v && v[0] >= '0' && v[0] <= '5' && v[1] == 0) ? v[0] - '0' : 5;
+        return !(v && v[0] == '0' && v[1] == 0);
     }();
-    return mode;
+    return on;
 }
 
 template <typename E, int R>
@@ -1085,15 +824,7 @@ int launch_lp_stream(const Geom &g, const E *e, E *eo, const E *rhs, cudaStream_
     switch (g.radius) {
         case 1: return run_lp<E, 1>(g, e, eo, rhs, s);
         case 2: return run_lp<E, 2>(g, e, eo, rhs, s);
-        case 4:
-            switch (lp_mma_mode()) {
-                case 0: return run_lp<E, 4>(g, e, eo, rhs, s);
-                case 1: return run_lp_tc<E, 1, 16, true, false>(g, e, eo, rhs, s);
-                case 2: return run_lp_tc<E, 2, 16, true, true>(g, e, eo, rhs, s);
-                case 3: return run_lp_tc<E, 2, 16, true, false>(g, e, eo, rhs, s);
-                case 4: return run_lp_tc<E, 1, 15, true, true>(g, e, eo, rhs, s);
-                default: return run_lp_tc3<E, 13>(g, e, eo, rhs, s);
-            }
+        case 4: return lp_mma_enabled() ? run_lp_tc3<E, 13>(g, e, eo, rhs, s) : run_lp<E, 4>(g, e, eo, rhs, s);
         default: return fail(STENCIL_EUNSUPPORTED, "low-precision stream kernel: R=%d", g.radius);
     }
 }

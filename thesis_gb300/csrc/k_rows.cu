@@ -71,6 +71,7 @@ __global__ void __launch_bounds__(128 * (TY / RY) + 32, 1)
                 const int s = q & (NS - 1);
                 const uint32_t use = q / NS;
                 if (use > 0 && !mbar_wait_bounded(&empty[s], (use - 1) & 1)) return;
+                fence_proxy_async();  // the consumers' reads of the slot before the bulk copy
                 mbar_arrive_expect_tx(&full[s], bytes);
                 const long long z = z0 - R + p;
                 bulk_load(ring + s * slotf + (ra - (y0 - R)) * nx,

@@ -135,6 +135,7 @@ __global__ void __launch_bounds__(StreamShape<R, TX, TY, RY, NS>::THREADS, Strea
                     const int s = q & (NS - 1);
                     const uint32_t use = q / NS;
                     if (use > 0 && !mbar_wait_bounded(&empty[s], (use - 1) & 1)) return;
+                    fence_proxy_async();  // the consumers' reads of the slot before the TMA write
                     mbar_arrive_expect_tx(&full[s], S::PLANE_BYTES);
                     tma_load_3d(ring + s * S::SLOT_FLOATS, src_map, &full[s], x0 - S::RA, y0 - R,
                                 z0 - R + p);

@@ -216,6 +216,7 @@ __global__ void __launch_bounds__(TbShape<R, T, TX, TY>::THREADS, 1)
                 const int s = seq % S::NS;
                 const uint32_t use = seq / S::NS;
                 if (use > 0 && !mbar_wait_bounded(&empty[s], (use - 1) & 1)) return;
+                fence_proxy_async();  // the consumers' reads of the slot before the TMA write
                 mbar_arrive_expect_tx(&full[s], S::PLANE_BYTES);
                 tma_load_3d(ring0 + s * S::SLOT_FLOATS, &src_map, &full[s], x0 - S::HX,
                             y0 - S::HY, p);
