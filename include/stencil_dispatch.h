@@ -239,7 +239,11 @@ STENCIL_API int stencil_batch_forget(const void *d_workspace);
  * Engines: 2-D grids of at most one tile per SM (R = 1, 2, 4) run each outer
  * step as one cooperative launch with every correction sweep in shared
  * memory (PERSISTENT_2D); other grids launch each correction sweep
- * (LAUNCHES).  Both give bit-identical results. */
+ * (LAUNCHES).  Both give bit-identical results.  3-D correction sweeps at
+ * R = 4 form their x- and y-neighbour sums on the tensor cores (products with
+ * banded matrices, FP32 accumulation: the same result up to FP32 roundings);
+ * the environment variable STENCIL_LP_MMA=0, read once per process, selects
+ * per-term adds instead. */
 enum { STENCIL_STORAGE_FP32 = 0, STENCIL_STORAGE_BF16 = 1, STENCIL_STORAGE_FP16 = 2 };
 enum {
     STENCIL_IR_ENGINE_AUTO = 0,          /* PERSISTENT_2D where it applies, else LAUNCHES */

@@ -29,7 +29,9 @@ namespace st {
 
 size_t residual_scratch_bytes();
 int launch_residual(const Geom &g, int dims, const float *u, double *scratch, cudaStream_t s);
-// The TMA-fed correction sweep for 3-D grids (k_lpstream.cu).
+// The TMA-fed correction sweep for 3-D grids (k_lpstream.cu): eo = M e + rhs
+// over the update region.  eo's border band must hold zeros (at R = 4 the
+// sweep's block stores write them there again); e and rhs are read only.
 bool lp_stream_supported(const Geom &g, int dims);
 template <typename E>
 int launch_lp_stream(const Geom &g, const E *e, E *eo, const E *rhs, cudaStream_t s);
