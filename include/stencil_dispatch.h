@@ -215,10 +215,43 @@ STENCIL_API int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, 
  * CUDA graph (the queue reset is a memset node, so every replay runs the
  * whole batch again; lanes become parallel branches). */
 STENCIL_API int stencil_batch_launch(const void *d_workspace, stencil_stream_t stream);
+/* Batch engines.  PHASED: what stencil_batch_launch describes above (a
+ * cluster launch, whole-GPU launches and lanes, the copy kernels).
+ * ONE_LAUNCH: every job in ONE persistent cooperative launch (one CTA per SM)
+ * -- the CTAs form teams, each team sweeps one grid at a time with all its
+ * sweeps (3-D grids with the stream kernel's TMA-ring code, 2-D grids with
+ * the rows kernel's register-queue code, a bounded barrier over the team
+ * between sweeps) and then takes the next grid from a device queue; grids
+ * are placed in tiers by the team size their cells keep busy (about
+ * STENCIL_BATCH1_CELLS_PER_CTA_2D = 100000 / _3D = 200000 update cells per
+ * CTA, at most STENCIL_BATCH1_MAX_TEAM = a quarter of the CTAs; environment
+ * variables of these names override them at prepare time), every team
+ * starts in the largest tier and splits into the next tier's teams when its
+ * queue is empty; ragged grids are copied in and out by their team inside the
+ * launch.  The tuning hints of stencil_batch_job are not used by it.  AUTO:
+ * the environment variable STENCIL_BATCH_ENGINE ("phased" or "one_launch")
+ * at prepare time, else PHASED. */
+#define STENCIL_BATCH_ENGINE_AUTO 0
+#define STENCIL_BATCH_ENGINE_PHASED 1
+#define STENCIL_BATCH_ENGINE_ONE_LAUNCH 2
+/* stencil_batch_prepare with a choice of engine (stencil_batch_prepare is
+ * this with STENCIL_BATCH_ENGINE_AUTO).  Re-preparing a workspace replaces
+ * its plan.  The workspace sizes above suffice for either engine. */
+STENCIL_API int stencil_batch_prepare_engine(const stencil_batch_job *jobs, int njobs, int engine,
+                                             int cluster_size, void *d_workspace,
+                                             size_t workspace_bytes, stencil_stream_t stream);
 /* How stencil_batch_launch runs a prepared workspace: *cluster_jobs jobs in
  * the cluster launch (none: no cluster launch), *whole_gpu_jobs jobs with a
- * launch of their own. */
+ * launch of their own (both 0 for the one-launch engine). */
 STENCIL_API int stencil_batch_plan(const void *d_workspace, int *cluster_jobs, int *whole_gpu_jobs);
+/* Kernel launches of one stencil_batch_launch of a prepared workspace (1 for
+ * the one-launch engine). */
+STENCIL_API int stencil_batch_launches(const void *d_workspace, int *kernel_launches);
+/* The one-launch engine's tiers: *tiers of them (0 for a phased workspace),
+ * the nominal team size and the job count of each of the first max_tiers in
+ * team_sizes / tier_jobs (either may be NULL). */
+STENCIL_API int stencil_batch_teams(const void *d_workspace, int *tiers, int *team_sizes,
+                                    int *tier_jobs, int max_tiers);
 /* *groups = how many sets of lanes run side by side (one per radius and
  * mode), *jobs = the jobs in them. */
 STENCIL_API int stencil_batch_side_by_side(const void *d_workspace, int *groups, int *jobs);

@@ -146,3 +146,25 @@ def test_reference_heuristic_block(stencil_lib, dims, variant, radius, block_x, 
     assert (bx.value, by.value, bz.value) == want
     assert stencil_lib.stencil_heuristic_block(ctypes.byref(p), 0, ctypes.byref(bx),
                                                ctypes.byref(by), ctypes.byref(bz)) != 0
+
+
+def test_batch_engine_choice_is_validated_without_device(stencil_lib):
+    """An unknown batch engine is refused before anything reaches a device,
+    and the workspace size covers either engine (job table, tensor maps,
+    team counters, pitched copies)."""
+    ws = ctypes.c_void_p(4096)
+    for engine in (-1, 3):
+        rc = stencil_lib.stencil_batch_prepare_engine(None, 0, engine, 0, ws, 1 << 20, None)
+        assert rc == L.EINVAL
+        assert b"engine" in stencil_lib.stencil_last_error()
+    small, big = ctypes.c_size_t(), ctypes.c_size_t()
+    assert stencil_lib.stencil_batch_workspace_bytes(1, ctypes.byref(small)) == L.OK
+    assert stencil_lib.stencil_batch_workspace_bytes(100, ctypes.byref(big)) == L.OK
+    assert big.value > small.value > 0
+    jobs = (L.BatchJob * 2)()
+    for j, (nx, ny, nz, d) in zip(jobs, [(66, 70, 1, 2), (41, 37, 43, 3)]):
+        j.dims, j.nx, j.ny, j.nz, j.radius, j.iterations = d, nx, ny, nz, 1, 1
+    need = ctypes.c_size_t()
+    assert stencil_lib.stencil_batch_workspace_bytes_for(jobs, 2, ctypes.byref(need)) == L.OK
+    # two pitched copies of each ragged grid at least
+    assert need.value >= 2 * 4 * (68 * 70 + 44 * 37 * 43)

@@ -1,0 +1,189 @@
+"""GPU parity of the one-launch batch engine (every grid of a batch in ONE
+persistent cooperative launch: teams of CTAs take grids from device queues,
+tier by tier), bit for bit against the oracle, with CUDA-graph replays."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def bits_equal(a, b):
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def oracle_pair(u, radius, iters, mode):
+    a, b = u.copy(), u.copy()
+    res = O.run(a, b, radius, mode, iters, threads=8)
+    return res, (b if res is a else a)
+
+
+# 2-D and 3-D, R = 1..4, JACOBI and LEGACY, ragged widths (swept in pitched
+# copies staged inside the launch), 0 and 1 sweeps, grids from a few cells
+# to a few million (teams of one CTA up to a quarter of the GPU).
+SPECS = [
+    ((64, 64), 1, 12, "jacobi"),
+    ((70, 66), 1, 23, "jacobi"),          # ragged
+    ((131, 127), 2, 9, "jacobi"),         # ragged
+    ((40, 36), 3, 6, "legacy"),
+    ((64, 64), 4, 5, "jacobi"),
+    ((9, 13), 4, 3, "jacobi"),            # the smallest 2-D grid at R = 4, ragged
+    ((200, 256), 1, 0, "jacobi"),         # no sweep: the result is d_u1 as given
+    ((256, 200), 2, 1, "legacy"),
+    ((1024, 1024), 1, 6, "jacobi"),
+    ((1500, 1301), 1, 5, "jacobi"),       # ragged
+    ((900, 640), 2, 5, "jacobi"),
+    ((700, 620), 4, 4, "legacy"),
+    ((30, 32, 32), 1, 12, "jacobi"),
+    ((37, 41, 43), 2, 11, "jacobi"),      # ragged
+    ((24, 20, 24), 2, 5, "legacy"),
+    ((20, 22, 26), 3, 4, "jacobi"),       # ragged
+    ((17, 18, 20), 4, 3, "jacobi"),
+    ((9, 9, 9), 4, 2, "jacobi"),          # the smallest 3-D grid at R = 4, ragged
+    ((96, 96, 96), 2, 4, "jacobi"),
+    ((120, 120, 120), 1, 9, "jacobi"),
+    ((150, 131, 141), 2, 7, "jacobi"),    # ragged
+    ((128, 128, 128), 1, 4, "legacy"),
+    ((160, 144, 128), 2, 6, "jacobi"),
+    ((100, 90, 88), 3, 3, "jacobi"),
+    ((96, 80, 72), 4, 3, "legacy"),
+]
+
+
+def _make(specs, seed0):
+    import torch
+    hosts, jobs, modes = [], [], []
+    for k, (shape, radius, iters, mode) in enumerate(specs):
+        u = O.uniform(shape, seed=seed0 + k)
+        m = O.JACOBI if mode == "jacobi" else O.LEGACY
+        hosts.append(u)
+        modes.append(m)
+        jobs.append((torch.from_numpy(u).cuda(), torch.from_numpy(u).cuda(), radius, iters, m))
+    return hosts, jobs, modes
+
+
+def _wants(specs, hosts, modes):
+    out = []
+    for k, (shape, radius, iters, _) in enumerate(specs):
+        out.append(oracle_pair(hosts[k], radius, iters, modes[k]))
+    return out
+
+
+def _check(b, specs, wants, jobs):
+    for k, (shape, radius, iters, _) in enumerate(specs):
+        want, other = wants[k]
+        res = b.result(k)
+        oth = jobs[k][1] if res is jobs[k][0] else jobs[k][0]
+        assert bits_equal(res.cpu().numpy(), want), (k, shape, radius, iters)
+        # the other buffer holds what the ping-pong loop leaves there
+        assert bits_equal(oth.cpu().numpy(), other), ("other buffer", k, shape, radius, iters)
+
+
+def _reset(jobs, hosts):
+    import torch
+    for k in range(len(jobs)):
+        jobs[k][0].copy_(torch.from_numpy(hosts[k]))
+        jobs[k][1].copy_(torch.from_numpy(hosts[k]))
+    torch.cuda.synchronize()
+
+
+# (STENCIL_BATCH1_CELLS_PER_CTA_2D, _3D, STENCIL_BATCH1_MAX_TEAM): the
+# defaults; every grid on a team of one CTA; every grid on the largest team
+# allowed; many tiers with small teams and remainders.
+TEAMS = [("", "", ""), ("1000000000", "1000000000", ""), ("1", "1", ""), ("5000", "7000", "16"),
+         ("", "", "1")]
+
+
+@pytest.mark.parametrize("cpc2,cpc3,maxteam", TEAMS)
+def test_one_launch_batch_matches_oracle_and_graph_replay(cuda, monkeypatch, cpc2, cpc3, maxteam):
+    import torch
+    from thesis_gb300 import stencil as S
+    monkeypatch.setenv("STENCIL_BATCH1_CELLS_PER_CTA_2D", cpc2)
+    monkeypatch.setenv("STENCIL_BATCH1_CELLS_PER_CTA_3D", cpc3)
+    monkeypatch.setenv("STENCIL_BATCH1_MAX_TEAM", maxteam)
+    hosts, jobs, modes = _make(SPECS, 500)
+    b = S.Batch(jobs, engine="one_launch")
+    assert b.kernel_launches() == 1
+    assert b.plan() == (0, 0)
+    tiers = b.teams()
+    assert sum(n for _, n in tiers) == len(SPECS)
+    assert all(t1 > t2 for (t1, _), (t2, _) in zip(tiers, tiers[1:]))  # largest teams first
+    if maxteam == "1" or cpc2 == "1000000000":
+        assert tiers == [(1, len(SPECS))]
+    b.launch()
+    torch.cuda.synchronize()
+    wants = _wants(SPECS, hosts, modes)
+    _check(b, SPECS, wants, jobs)
+    # captured into a CUDA graph (a memset node and one kernel node), replayed
+    # twice from reset inputs: the queues and team counters start afresh
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            b.launch(stream=s)
+    for _ in range(2):
+        _reset(jobs, hosts)
+        g.replay()
+        torch.cuda.synchronize()
+        _check(b, SPECS, wants, jobs)
+    b.close()
+    assert S.device_status() == 0
+
+
+def test_one_launch_batch_engines_agree_on_benchmark_like_mix(cuda):
+    """A scaled-down mix of the 512-grid benchmark batch (2-D R = 1 sides
+    log-uniform, 3-D R = 2 sides log-uniform, sweeps uniform): both engines
+    give bit-identical results, and the one-launch result matches the oracle
+    on a sample."""
+    import torch
+    from thesis_gb300 import stencil as S
+    rng = np.random.default_rng(77)
+    specs = []
+    for _ in range(40):
+        n = int(round(np.exp(rng.uniform(np.log(64), np.log(1024)))))
+        specs.append(((n, n), 1, int(rng.integers(1, 40)), "jacobi"))
+    for _ in range(12):
+        n = int(round(np.exp(rng.uniform(np.log(32), np.log(160)))))
+        specs.append(((n, n, n), 2, int(rng.integers(1, 20)), "jacobi"))
+    hosts, jobs1, modes = _make(specs, 900)
+    _, jobs2, _ = _make(specs, 900)
+    b1 = S.Batch(jobs1, engine="one_launch")
+    b2 = S.Batch(jobs2, engine="phased")
+    b1.launch()
+    b2.launch()
+    torch.cuda.synchronize()
+    for k in range(len(specs)):
+        assert bits_equal(b1.result(k).cpu().numpy(), b2.result(k).cpu().numpy()), (k, specs[k])
+    for k in range(0, len(specs), 5):
+        want, _ = oracle_pair(hosts[k], specs[k][1], specs[k][2], modes[k])
+        assert bits_equal(b1.result(k).cpu().numpy(), want), (k, specs[k])
+    b1.close()
+    b2.close()
+    assert S.device_status() == 0
+
+
+def test_one_launch_batch_reprepare_and_env_engine(cuda, monkeypatch):
+    """STENCIL_BATCH_ENGINE=one_launch makes "auto" the one-launch engine; a
+    workspace prepared again with the other engine follows the new plan."""
+    import torch
+    from thesis_gb300 import lib as L
+    from thesis_gb300 import stencil as S
+    specs = SPECS[:6] + SPECS[12:16]
+    hosts, jobs, modes = _make(specs, 700)
+    monkeypatch.setenv("STENCIL_BATCH_ENGINE", "one_launch")
+    b = S.Batch(jobs)
+    assert b.kernel_launches() == 1 and b.teams()
+    monkeypatch.setenv("STENCIL_BATCH_ENGINE", "phased")
+    b2 = S.Batch(jobs)
+    assert b2.teams() == []
+    b.launch()
+    torch.cuda.synchronize()
+    _check(b, specs, _wants(specs, hosts, modes), jobs)
+    b.close()
+    b2.close()
+    lib = L.load()
+    rc = lib.stencil_batch_prepare_engine(None, 0, 3, 0, b.workspace.data_ptr(), 0, None)
+    assert rc == L.EINVAL

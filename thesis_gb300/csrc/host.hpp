@@ -62,6 +62,10 @@ int run_stream3d(const Geom &g, float *a, float *b, int iters, int tile_x, int t
                  int max_ctas = 0);
 // CTAs of the device that the persistent stream kernel for g can hold at once.
 int stream3d_capacity(const Geom &g, int *ctas);
+// Work items of a stream sweep of g with tx x ty tiles on `resident` CTAs:
+// tiles along x and y, planes per z-chunk, (tile, z-chunk) items.
+void stream3d_plan(const Geom &g, int tx, int ty, int resident, int *tiles_x, int *tiles_y,
+                   int *zchunk, int *items);
 int run_tb3d(const Geom &g, float *a, float *b, int iters, int temporal, cudaStream_t s,
              float **res);
 // A zeroed grid-barrier counter for one persistent launch on stream s
@@ -81,6 +85,9 @@ void tb2d_release();
 // device that the kernel for g's radius can hold at once.
 bool rows2d_supported(const Geom &g, int dims);
 int rows2d_capacity(const Geom &g);
+// Row blocks of a rows sweep of g on `threads` threads: *hb rows per block,
+// *nblk blocks.
+void rows2d_plan(const Geom &g, long long threads, int *hb, int *nblk);
 int run_rows2d(const Geom &g, float *a, float *b, int iters, cudaStream_t s, float **res,
                int max_ctas = 0);
 // All sweeps of one grid on one thread-block cluster (k_cluster.cu).
@@ -91,6 +98,19 @@ bool cluster_resident(const Geom &g, int dims);
 // The cluster engine takes the shape (nx % 4 == 0, R <= 4, 3-D planes of
 // fewer than 2^31 float4 chunks).
 bool cluster_shape_ok(int dims, int px, int ny, int radius);
+
+// Batches (k_cluster.cu, k_batch1.cu).  check_batch_job: the checks every
+// batch job passes, *out its parameters.  batch1_*: the one-launch engine
+// (prepare writes the job table, tensor maps and tiers into the workspace and
+// remembers the plan; launch = a memset node and one cooperative kernel).
+int check_batch_job(const stencil_batch_job &b, int i, stencil_params *out);
+size_t batch1_bytes_for(const stencil_batch_job *jobs, int njobs);
+int batch1_prepare(const stencil_batch_job *jobs, int njobs, void *d_workspace,
+                   size_t workspace_bytes, cudaStream_t s);
+bool batch1_known(const void *d_workspace);
+int batch1_launch(const void *d_workspace, cudaStream_t s);
+int batch1_teams(const void *d_workspace, int *ntiers, int *team_sizes, int *tier_jobs, int max_tiers);
+void batch1_forget(const void *d_workspace);
 
 // Mixed-precision refinement, persistent 2-D form of an outer step
 // (k_ir2d.cu): one CTA per tile, T correction sweeps per halo exchange.

@@ -34,6 +34,7 @@
 #include <cstdlib>
 #include <memory>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "host.hpp"
@@ -989,28 +990,86 @@ size_t batch_bytes_for(const stencil_batch_job *jobs, int njobs) {
 
 }  // namespace
 
+// The checks every batch job passes (either engine): valid parameters, two
+// distinct 16-byte aligned buffers, radius <= 4, tuning fields in range.
+int check_batch_job(const stencil_batch_job &b, int i, stencil_params *out) {
+    stencil_params p;
+    stencil_params_init(&p);
+    p.dims = b.dims; p.nx = b.nx; p.ny = b.ny; p.nz = b.dims == 3 ? b.nz : 1;
+    p.radius = b.radius; p.iterations = b.iterations; p.mode = b.mode;
+    int rc = stencil_params_check(&p);
+    if (rc) return fail(rc, "job %d: %s", i, stencil_last_error());
+    if (!b.d_u1 || !b.d_u2 || b.d_u1 == b.d_u2 ||
+        ((reinterpret_cast<uintptr_t>(b.d_u1) | reinterpret_cast<uintptr_t>(b.d_u2)) & 15))
+        return fail(STENCIL_EINVAL, "job %d: two distinct 16-byte aligned buffers required", i);
+    const int px = (b.nx + 3) & ~3;
+    if (!cluster_job_ok(b.dims, px, b.ny, b.nz, b.radius))
+        return fail(STENCIL_EUNSUPPORTED, "job %d: batch jobs need radius <= 4", i);
+    if (b.temporal < 0 || b.tile_x < 0 || b.tile_y < 0 || (b.tile_x % 4) || b.reserved[0] ||
+        b.reserved[1] || b.reserved[2])
+        return fail(STENCIL_EINVAL,
+                    "job %d: temporal, tile_x, tile_y >= 0, tile_x %% 4 == 0, reserved zero", i);
+    *out = p;
+    return STENCIL_OK;
+}
+
 }  // namespace st
 
 using namespace st;
 
 extern "C" int stencil_batch_workspace_bytes(int njobs, size_t *bytes) {
     if (njobs < 0 || !bytes) return fail(STENCIL_EINVAL, "bad arguments");
-    *bytes = batch_bytes(njobs);
+    // enough for either engine: the one-launch engine's table with every job
+    // 3-D (two tensor maps each)
+    std::vector<stencil_batch_job> any(njobs);
+    for (auto &j : any) { j = stencil_batch_job{}; j.dims = 3; j.nx = 4; j.ny = 1; }
+    *bytes = std::max(batch_bytes(njobs), batch1_bytes_for(any.data(), njobs));
     return STENCIL_OK;
 }
 
 extern "C" int stencil_batch_workspace_bytes_for(const stencil_batch_job *jobs, int njobs,
                                                  size_t *bytes) {
     if (njobs < 0 || (njobs && !jobs) || !bytes) return fail(STENCIL_EINVAL, "bad arguments");
-    *bytes = batch_bytes_for(jobs, njobs);
+    *bytes = std::max(batch_bytes_for(jobs, njobs), batch1_bytes_for(jobs, njobs));
     return STENCIL_OK;
 }
+
+namespace st {
+namespace {
+// The engine STENCIL_BATCH_ENGINE_AUTO stands for: the environment variable
+// STENCIL_BATCH_ENGINE ("phased" or "one_launch") read at prepare time, else
+// the phased engine.
+int batch_engine_auto() {
+    const char *e = std::getenv("STENCIL_BATCH_ENGINE");
+    if (e && std::string(e) == "one_launch") return STENCIL_BATCH_ENGINE_ONE_LAUNCH;
+    return STENCIL_BATCH_ENGINE_PHASED;
+}
+}  // namespace
+}  // namespace st
 
 extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, int cluster_size,
                                      void *d_workspace, size_t workspace_bytes,
                                      stencil_stream_t stream) {
+    return stencil_batch_prepare_engine(jobs, njobs, STENCIL_BATCH_ENGINE_AUTO, cluster_size,
+                                        d_workspace, workspace_bytes, stream);
+}
+
+extern "C" int stencil_batch_prepare_engine(const stencil_batch_job *jobs, int njobs, int engine,
+                                            int cluster_size, void *d_workspace,
+                                            size_t workspace_bytes, stencil_stream_t stream) {
     if (njobs < 0 || (njobs && !jobs) || !d_workspace)
         return fail(STENCIL_EINVAL, "bad arguments");
+    if (engine < STENCIL_BATCH_ENGINE_AUTO || engine > STENCIL_BATCH_ENGINE_ONE_LAUNCH)
+        return fail(STENCIL_EINVAL, "unknown batch engine %d", engine);
+    if (engine == STENCIL_BATCH_ENGINE_AUTO) engine = batch_engine_auto();
+    if (engine == STENCIL_BATCH_ENGINE_ONE_LAUNCH) {
+        if (reinterpret_cast<uintptr_t>(d_workspace) & 255)
+            return fail(STENCIL_EINVAL, "workspace must be 256-byte aligned");
+        stencil_batch_forget(d_workspace);
+        return batch1_prepare(jobs, njobs, d_workspace, workspace_bytes,
+                              reinterpret_cast<cudaStream_t>(stream));
+    }
+    batch1_forget(d_workspace);
     if (workspace_bytes < batch_bytes_for(jobs, njobs))
         return fail(STENCIL_EINVAL,
                     "workspace too small: %zu < %zu bytes (stencil_batch_workspace_bytes_for "
@@ -1036,21 +1095,9 @@ extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, i
     for (int i = 0; i < njobs; ++i) {
         const stencil_batch_job &b = jobs[i];
         stencil_params p;
-        stencil_params_init(&p);
-        p.dims = b.dims; p.nx = b.nx; p.ny = b.ny; p.nz = b.dims == 3 ? b.nz : 1;
-        p.radius = b.radius; p.iterations = b.iterations; p.mode = b.mode;
-        int rc = stencil_params_check(&p);
-        if (rc) return fail(rc, "job %d: %s", i, stencil_last_error());
-        if (!b.d_u1 || !b.d_u2 || b.d_u1 == b.d_u2 ||
-            ((reinterpret_cast<uintptr_t>(b.d_u1) | reinterpret_cast<uintptr_t>(b.d_u2)) & 15))
-            return fail(STENCIL_EINVAL, "job %d: two distinct 16-byte aligned buffers required", i);
+        int rc = check_batch_job(b, i, &p);
+        if (rc) return rc;
         const int px = (b.nx + 3) & ~3;
-        if (!cluster_job_ok(b.dims, px, b.ny, b.nz, b.radius))
-            return fail(STENCIL_EUNSUPPORTED, "job %d: batch jobs need radius <= 4", i);
-        if (b.temporal < 0 || b.tile_x < 0 || b.tile_y < 0 || (b.tile_x % 4) || b.reserved[0] ||
-            b.reserved[1] || b.reserved[2])
-            return fail(STENCIL_EINVAL,
-                        "job %d: temporal, tile_x, tile_y >= 0, tile_x %% 4 == 0, reserved zero", i);
         Geom g = make_geom(p);
         float *ga = b.d_u1, *gb = b.d_u2;
         if (px != b.nx) {
@@ -1119,6 +1166,7 @@ extern "C" int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, i
 extern "C" int stencil_batch_launch(const void *d_workspace, stencil_stream_t stream) {
     if (!d_workspace) return fail(STENCIL_EINVAL, "null workspace");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (batch1_known(d_workspace)) return batch1_launch(d_workspace, s);
     BatchPlan plan;
     if (!recall(d_workspace, &plan))
         return fail(STENCIL_EINVAL, "workspace was not prepared by stencil_batch_prepare");
@@ -1174,6 +1222,10 @@ extern "C" int stencil_batch_launch(const void *d_workspace, stencil_stream_t st
 
 extern "C" int stencil_batch_plan(const void *d_workspace, int *cluster_jobs, int *whole_gpu_jobs) {
     if (!d_workspace || !cluster_jobs || !whole_gpu_jobs) return fail(STENCIL_EINVAL, "null argument");
+    if (batch1_known(d_workspace)) {
+        *cluster_jobs = *whole_gpu_jobs = 0;
+        return STENCIL_OK;
+    }
     BatchPlan plan;
     if (!recall(d_workspace, &plan))
         return fail(STENCIL_EINVAL, "workspace was not prepared by stencil_batch_prepare");
@@ -1184,10 +1236,11 @@ extern "C" int stencil_batch_plan(const void *d_workspace, int *cluster_jobs, in
 
 extern "C" int stencil_batch_side_by_side(const void *d_workspace, int *groups, int *jobs) {
     if (!d_workspace || !groups || !jobs) return fail(STENCIL_EINVAL, "null argument");
+    *groups = *jobs = 0;
+    if (batch1_known(d_workspace)) return STENCIL_OK;
     BatchPlan plan;
     if (!recall(d_workspace, &plan))
         return fail(STENCIL_EINVAL, "workspace was not prepared by stencil_batch_prepare");
-    *groups = *jobs = 0;
     for (const BatchPlan::Phase &ph : plan.phases)
         if (ph.queue.size() > 1) {
             ++*groups;
@@ -1196,7 +1249,31 @@ extern "C" int stencil_batch_side_by_side(const void *d_workspace, int *groups, 
     return STENCIL_OK;
 }
 
+extern "C" int stencil_batch_launches(const void *d_workspace, int *kernel_launches) {
+    if (!d_workspace || !kernel_launches) return fail(STENCIL_EINVAL, "null argument");
+    if (batch1_known(d_workspace)) {
+        *kernel_launches = 1;
+        return STENCIL_OK;
+    }
+    BatchPlan plan;
+    if (!recall(d_workspace, &plan))
+        return fail(STENCIL_EINVAL, "workspace was not prepared by stencil_batch_prepare");
+    *kernel_launches = (plan.h.njobs ? 1 : 0) + (int)plan.streamed.size() + (plan.nstaged ? 2 : 0);
+    return STENCIL_OK;
+}
+
+extern "C" int stencil_batch_teams(const void *d_workspace, int *tiers, int *team_sizes,
+                                   int *tier_jobs, int max_tiers) {
+    if (!d_workspace || !tiers) return fail(STENCIL_EINVAL, "null argument");
+    if (!batch1_known(d_workspace)) {
+        *tiers = 0;
+        return STENCIL_OK;
+    }
+    return batch1_teams(d_workspace, tiers, team_sizes, tier_jobs, max_tiers);
+}
+
 extern "C" int stencil_batch_forget(const void *d_workspace) {
+    batch1_forget(d_workspace);
     std::lock_guard<std::mutex> lock(g_batch_mu);
     for (size_t i = 0; i < g_batch.size(); ++i)
         if (g_batch[i].first == d_workspace) {

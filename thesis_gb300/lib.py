@@ -122,6 +122,9 @@ def load() -> ctypes.CDLL:
         "stencil_batch_forget": (i, [vp]),
         "stencil_batch_plan": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(i)]),
         "stencil_batch_side_by_side": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(i)]),
+        "stencil_batch_prepare_engine": (i, [ctypes.POINTER(BatchJob), i, i, i, vp, sz, vp]),
+        "stencil_batch_launches": (i, [vp, ctypes.POINTER(i)]),
+        "stencil_batch_teams": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i), i]),
         "stencil_ir_workspace_bytes": (i, [P, ctypes.POINTER(IrParams), ctypes.POINTER(sz)]),
         "stencil_ir_solve": (i, [P, ctypes.POINTER(IrParams), vp, vp, sz, vp,
                                  ctypes.POINTER(IrResult)]),

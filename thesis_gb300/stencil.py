@@ -231,8 +231,12 @@ def device_status() -> int:
 
 
 class Batch:
-    """Many grids of uneven sizes and sweep counts in one persistent launch
-    (stencil_batch_prepare / stencil_batch_launch).
+    """Many grids of uneven sizes and sweep counts in persistent launches
+    (stencil_batch_prepare_engine / stencil_batch_launch).
+
+    engine: "one_launch" (every job in ONE cooperative launch, teams of CTAs
+    taking grids from device queues), "phased" (a cluster launch, then
+    whole-GPU launches and lanes) or "auto" (the library's choice).
 
     jobs: list of (d_u1, d_u2, radius, iterations, mode[, hints]) with CUDA
     float32 tensors of shape (ny, nx) or (nz, ny, nx); hints (optional dict)
@@ -243,7 +247,9 @@ class Batch:
     d_u2 (``result(i)``).
     """
 
-    def __init__(self, jobs, cluster_size: int = 0, stream=None, hints_for=None):
+    ENGINES = {"auto": 0, "phased": 1, "one_launch": 2}
+
+    def __init__(self, jobs, cluster_size: int = 0, stream=None, hints_for=None, engine: str = "auto"):
         import torch
         self.jobs = [tuple(j[:5]) for j in jobs]
         hints = [j[5] if len(j) > 5 else None for j in jobs]
@@ -270,9 +276,9 @@ class Batch:
         self.workspace = torch.empty(nbytes.value + 256, dtype=torch.uint8, device=dev)
         base = self.workspace.data_ptr()
         self.ws = ctypes.c_void_p((base + 255) & ~255)
-        _lib.check(L.stencil_batch_prepare(arr, len(self.jobs), cluster_size, self.ws,
-                                           nbytes.value, _stream_handle(stream)),
-                   "stencil_batch_prepare")
+        _lib.check(L.stencil_batch_prepare_engine(arr, len(self.jobs), self.ENGINES[engine], cluster_size,
+                                                  self.ws, nbytes.value, _stream_handle(stream)),
+                   "stencil_batch_prepare_engine")
 
     def launch(self, stream=None):
         _lib.check(_lib.load().stencil_batch_launch(self.ws, _stream_handle(stream)),
@@ -295,11 +301,21 @@ class Batch:
 
     def kernel_launches(self):
         """Kernel launches of one ``launch`` (one replay of its CUDA graph):
-        the cluster launch, one per whole-GPU job, and the two copy kernels
-        of jobs whose nx is not a multiple of 4."""
-        c, w = self.plan()
-        ragged = any(u1.shape[-1] % 4 for u1, *_ in self.jobs)
-        return (1 if c else 0) + w + (2 if ragged else 0)
+        1 for the one-launch engine; for the phased one the cluster launch,
+        one per whole-GPU job, and the two copy kernels of jobs whose nx is
+        not a multiple of 4."""
+        n = ctypes.c_int()
+        _lib.check(_lib.load().stencil_batch_launches(self.ws, ctypes.byref(n)), "stencil_batch_launches")
+        return n.value
+
+    def teams(self):
+        """The one-launch engine's tiers as [(nominal team size, jobs)], largest
+        teams first ([] for the phased engine)."""
+        n = ctypes.c_int()
+        sizes, counts = (ctypes.c_int * 16)(), (ctypes.c_int * 16)()
+        _lib.check(_lib.load().stencil_batch_teams(self.ws, ctypes.byref(n), sizes, counts, 16),
+                   "stencil_batch_teams")
+        return [(sizes[t], counts[t]) for t in range(min(n.value, 16))]
 
     def result(self, k):
         u1, u2, _, iters, _ = self.jobs[k]
