@@ -462,10 +462,13 @@ def c4_jobs(seed=20251204):
 
 
 def bench_c4(S, lib, torch):
-    """512 grids of uneven sizes and sweep counts, replayed as one CUDA graph:
-    one persistent cluster launch over a device work queue for the grids a
-    cluster sweeps, then one whole-GPU persistent launch per 3-D grid too large
-    for a cluster's shared memory; cluster size picked by the autotuner."""
+    """512 grids of uneven sizes and sweep counts.  The line item: the
+    one-launch engine -- every grid in ONE cooperative launch, teams of CTAs
+    taking grids from device queues -- replayed as a CUDA graph.  Beside it
+    the phased engine (a persistent cluster launch over a device work queue
+    for the grids a cluster sweeps, then persistent whole-GPU launches in
+    lanes), with its cluster size and per-class hints picked by the
+    autotuner."""
     from thesis_gb300 import autotune as A
     specs = c4_jobs()
     ups = 0.0
@@ -478,6 +481,32 @@ def bench_c4(S, lib, torch):
     for k, (shape, R, it) in enumerate(specs):
         u = S.init_uniform(shape, SEED + k)
         grids.append((u, u.clone()))
+
+    def timed(bt, reps=3):
+        stream = torch.cuda.Stream()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(stream):
+            bt.launch(stream=stream)  # warm-up
+            stream.synchronize()
+            with torch.cuda.graph(graph, stream=stream):
+                bt.launch(stream=stream)
+        times = []
+        with torch.cuda.stream(stream):
+            for _ in range(reps):
+                e0, e1 = _events(torch)
+                e0.record(stream)
+                graph.replay()  # replays on the current stream
+                e1.record(stream)
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1) / 1e3)
+        del graph
+        return min(times)
+
+    jobs = [(g[0], g[1], sp[1], sp[2], lib.MODE_JACOBI) for g, sp in zip(grids, specs)]
+    b1 = S.Batch(jobs, engine="one_launch")
+    t1 = timed(b1)
+    launches1, teams = b1.kernel_launches(), b1.teams()
+    b1.close()
 
     def sample_jobs():
         # every 8th grid, sweeps / 10: a proxy of the batch for the tuner
@@ -494,26 +523,10 @@ def bench_c4(S, lib, torch):
                  max(10, specs[k][2] // 10), lib.MODE_JACOBI) for k in ks]
 
     tuned = A.tune_batch(class_jobs, log=None)
-    jobs = [(g[0], g[1], sp[1], sp[2], lib.MODE_JACOBI) for g, sp in zip(grids, specs)]
-    bt = S.Batch(jobs, cluster_size=csize, hints_for=A.batch_hints({"batch": tuned}))
-    stream = torch.cuda.Stream()
-    graph = torch.cuda.CUDAGraph()
-    with torch.cuda.stream(stream):
-        bt.launch(stream=stream)  # warm-up
-        stream.synchronize()
-        with torch.cuda.graph(graph, stream=stream):
-            bt.launch(stream=stream)
+    bt = S.Batch(jobs, cluster_size=csize, hints_for=A.batch_hints({"batch": tuned}), engine="phased")
+    tp = timed(bt)
     cluster_jobs, whole_gpu_jobs = bt.plan()
     launches = bt.kernel_launches()
-    times = []
-    with torch.cuda.stream(stream):
-        for _ in range(3):
-            e0, e1 = _events(torch)
-            e0.record(stream)
-            graph.replay()  # replays on the current stream
-            e1.record(stream)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1) / 1e3)
     bt.close()
     mem = sum(g[0].numel() * 8 for g in grids)
     del grids, jobs
@@ -521,12 +534,15 @@ def bench_c4(S, lib, torch):
     ragged = sum(1 for shape, _, _ in specs if shape[-1] % 4)
     return {"workload": "512 grids: 384 2D R=1 side 64..2048 + 128 3D R=2 side 32..256, 100..5000 sweeps",
             "ragged_jobs": ragged,
-            "value": round(ups / min(times) / 1e9, 2), "unit": "GCell-updates/s",
-            "s_per_batch": round(min(times), 3), "cell_updates": ups, "cluster_size": csize,
-            "device_bytes": mem, "graph_replays_per_batch": 1, "kernel_launches_per_batch": launches,
-            "cluster_jobs": cluster_jobs, "whole_gpu_jobs": whole_gpu_jobs, "graph": True,
-            "tuned": {c: r["choice"] for c, r in tuned.items()},
-            "roofline_frac_if_hbm": round(ups / min(times) * 8 / 1e9 / peaks()[0], 4)}
+            "value": round(ups / t1 / 1e9, 2), "unit": "GCell-updates/s",
+            "s_per_batch": round(t1, 3), "cell_updates": ups, "engine": "one_launch",
+            "device_bytes": mem, "graph_replays_per_batch": 1, "kernel_launches_per_batch": launches1,
+            "teams": [{"team_ctas": t, "jobs": n} for t, n in teams], "graph": True,
+            "roofline_frac_if_hbm": round(ups / t1 * 8 / 1e9 / peaks()[0], 4),
+            "phased": {"value": round(ups / tp / 1e9, 2), "s_per_batch": round(tp, 3),
+                       "kernel_launches_per_batch": launches, "cluster_jobs": cluster_jobs,
+                       "whole_gpu_jobs": whole_gpu_jobs, "cluster_size": csize,
+                       "tuned": {c: r["choice"] for c, r in tuned.items()}}}
 
 
 def bench_c5(W, torch, seeds):
@@ -764,7 +780,7 @@ def _profile_case(case):
             n = 64 + 32 * (k % 8)
             u = S.init_uniform((n, n), k)
             jobs.append((u, u.clone(), 1, 200 + 10 * k, J))
-        bt = S.Batch(jobs)
+        bt = S.Batch(jobs, engine="phased")
         for _ in range(3):
             bt.launch()
     elif case == "batch_3d_small":
@@ -775,7 +791,7 @@ def _profile_case(case):
         for k, n in enumerate(sides):
             u = S.init_uniform((n, n, n), k)
             jobs.append((u, u.clone(), 2, 100, J))
-        bt = S.Batch(jobs)
+        bt = S.Batch(jobs, engine="phased")
         for _ in range(3):
             bt.launch()
         cells = sum((n - 4) ** 3 * 100 for n in sides)
@@ -788,6 +804,41 @@ def _profile_case(case):
             e1.synchronize()
             best = min(best, e0.elapsed_time(e1))
         print("batch_3d_small: %.3f ms, %.1f GCell-updates/s" % (best, cells / best / 1e6))
+    elif case == "batch_one_launch_mix":
+        # a scaled-down mix of the benchmark batch in the one-launch engine:
+        # 48 2-D R=1 grids (sides 64..1024, about half ragged) and 16 3-D R=2
+        # grids (sides 32..160), 40..200 sweeps; one kernel per launch, about
+        # 0.3 GB on the device
+        import numpy as np
+        rng = np.random.default_rng(5)
+        jobs, cells = [], 0
+        for k in range(64):
+            if k < 48:
+                n, R = int(round(np.exp(rng.uniform(np.log(64), np.log(1024))))), 1
+                shape = (n, n)
+            else:
+                n, R = int(round(np.exp(rng.uniform(np.log(32), np.log(160))))), 2
+                shape = (n, n, n)
+            it = int(rng.integers(40, 201))
+            u = S.init_uniform(shape, k)
+            jobs.append((u, u.clone(), R, it, J))
+            c = it
+            for d in shape:
+                c *= d - 2 * R
+            cells += c
+        bt = S.Batch(jobs, engine="one_launch")
+        for _ in range(3):
+            bt.launch()
+        best = 1e30
+        for _ in range(5):
+            e0, e1 = _events(torch)
+            e0.record()
+            bt.launch()
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        print("batch_one_launch_mix: %.3f ms, %.1f GCell-updates/s, %d kernel per launch"
+              % (best, cells / best / 1e6, bt.kernel_launches()))
     else:
         raise SystemExit("unknown profile case " + case)
     torch.cuda.synchronize()

@@ -196,7 +196,10 @@ STENCIL_API int stencil_batch_workspace_bytes_for(const stencil_batch_job *jobs,
 STENCIL_API int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, int cluster_size,
                                       void *d_workspace, size_t workspace_bytes,
                                       stencil_stream_t stream);
-/* Runs the prepared jobs: the copies of ragged jobs in (one kernel), one
+/* Runs the prepared jobs with the engine chosen at prepare time (see the
+ * engines below).  The one-launch engine: a memset node (its queues and
+ * counters) and one cooperative kernel.  The phased engine: the copies of
+ * ragged jobs in (one kernel), one
  * persistent cluster launch over a device work queue (every cluster the
  * device can hold) for the jobs that a cluster sweeps, then, for each job too
  * large for a cluster's shared memory, one persistent launch of its own, and
@@ -216,21 +219,23 @@ STENCIL_API int stencil_batch_prepare(const stencil_batch_job *jobs, int njobs, 
  * whole batch again; lanes become parallel branches). */
 STENCIL_API int stencil_batch_launch(const void *d_workspace, stencil_stream_t stream);
 /* Batch engines.  PHASED: what stencil_batch_launch describes above (a
- * cluster launch, whole-GPU launches and lanes, the copy kernels).
+ * cluster launch, whole-GPU launches and lanes, the copy kernels; it applies
+ * the jobs' tuning hints).
  * ONE_LAUNCH: every job in ONE persistent cooperative launch (one CTA per SM)
  * -- the CTAs form teams, each team sweeps one grid at a time with all its
  * sweeps (3-D grids with the stream kernel's TMA-ring code, 2-D grids with
  * the rows kernel's register-queue code, a bounded barrier over the team
  * between sweeps) and then takes the next grid from a device queue; grids
  * are placed in tiers by the team size their cells keep busy (about
- * STENCIL_BATCH1_CELLS_PER_CTA_2D = 100000 / _3D = 200000 update cells per
+ * STENCIL_BATCH1_CELLS_PER_CTA_2D = 50000 / _3D = 50000 update cells per
  * CTA, at most STENCIL_BATCH1_MAX_TEAM = a quarter of the CTAs; environment
  * variables of these names override them at prepare time), every team
  * starts in the largest tier and splits into the next tier's teams when its
  * queue is empty; ragged grids are copied in and out by their team inside the
  * launch.  The tuning hints of stencil_batch_job are not used by it.  AUTO:
  * the environment variable STENCIL_BATCH_ENGINE ("phased" or "one_launch")
- * at prepare time, else PHASED. */
+ * at prepare time, else PHASED when some job carries tuning hints, else
+ * ONE_LAUNCH. */
 #define STENCIL_BATCH_ENGINE_AUTO 0
 #define STENCIL_BATCH_ENGINE_PHASED 1
 #define STENCIL_BATCH_ENGINE_ONE_LAUNCH 2

@@ -45,7 +45,7 @@ def test_batch_hints_bit_exact(cuda, specs, hint):
     from thesis_gb300 import stencil as S
     jobs = _jobs(specs)
     hosts = [j[0].cpu().numpy() for j in jobs]
-    bt = S.Batch([j + (hint,) for j in jobs])
+    bt = S.Batch([j + (hint,) for j in jobs], engine="phased")
     bt.launch()
     _check(bt, jobs, hosts)
     bt.close()
@@ -74,7 +74,7 @@ def test_tune_batch_and_apply(cuda):
     db = {"batch": res}
     jobs = _jobs(specs["2d_small"] + specs["3d_large"], seed=9)
     hosts = [j[0].cpu().numpy() for j in jobs]
-    bt = S.Batch(jobs, hints_for=A.batch_hints(db))
+    bt = S.Batch(jobs, hints_for=A.batch_hints(db), engine="phased")
     bt.launch()
     _check(bt, jobs, hosts)
     bt.close()

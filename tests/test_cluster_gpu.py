@@ -94,7 +94,7 @@ def test_batch_matches_oracle_and_graph_replay(cuda, cluster_size):
         u = O.uniform(shape, seed=100 + k)
         hosts.append(u)
         jobs.append((torch.from_numpy(u).cuda(), torch.from_numpy(u).cuda(), radius, iters, O.JACOBI))
-    b = S.Batch(jobs, cluster_size=cluster_size)
+    b = S.Batch(jobs, cluster_size=cluster_size, engine="phased")
     b.launch()
     torch.cuda.synchronize()
     wants = []
@@ -149,7 +149,7 @@ def test_batch_ragged_sides_match_oracle_and_graph_replay(cuda):
         u = O.uniform(shape, seed=300 + k)
         hosts.append(u)
         jobs.append((torch.from_numpy(u).cuda(), torch.from_numpy(u).cuda(), radius, iters, O.JACOBI))
-    b = S.Batch(jobs)
+    b = S.Batch(jobs, engine="phased")
     b.launch()
     torch.cuda.synchronize()
     wants = []
@@ -215,7 +215,7 @@ def test_batch_lanes_mid_size_3d_jobs(cuda, monkeypatch, lanes, cap, expect):
         hosts.append(u)
         modes.append(m)
         jobs.append((torch.from_numpy(u).cuda(), torch.from_numpy(u).cuda(), radius, iters, m))
-    b = S.Batch(jobs)
+    b = S.Batch(jobs, engine="phased")
     assert b.plan() == (0, len(PAIRED))
     assert b.side_by_side() == expect
     b.launch()

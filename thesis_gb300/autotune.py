@@ -214,7 +214,7 @@ def tune_batch_cluster_size(make_jobs, sizes=(1, 2, 4, 8, 16), log=print):
     for c in sizes:
         jobs = make_jobs()
         try:
-            bt = S.Batch(jobs, cluster_size=c)
+            bt = S.Batch(jobs, cluster_size=c, engine="phased")
         except _lib.StencilError:
             continue
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -295,7 +295,7 @@ def tune_batch(make_jobs, classes=None, repeats=2, log=print):
                     job[0].copy_(u1)
                     job[1].copy_(u2)
                 try:
-                    bt = S.Batch([tuple(j[:5]) + (hint,) for j in jobs])
+                    bt = S.Batch([tuple(j[:5]) + (hint,) for j in jobs], engine="phased")
                 except _lib.StencilError:
                     return float("inf")
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

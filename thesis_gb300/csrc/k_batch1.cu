@@ -43,29 +43,48 @@
 namespace st {
 namespace {
 
-// Stream shapes of the batch kernel per radius (the persistent single-grid
-// defaults: 16 one-row consumer warps + a producer warp at R = 1, 3, 4;
-// 128 x 32 tiles with two rows per thread at R = 2); all 544 threads.
-template <int R> struct B1S;
-template <> struct B1S<1> { static constexpr int TX = 128, TY = 16, RY = 1, NS = 16; };
-template <> struct B1S<2> { static constexpr int TX = 128, TY = 16, RY = 1, NS = 16; };
-template <> struct B1S<3> { static constexpr int TX = 128, TY = 16, RY = 1, NS = 8; };
-template <> struct B1S<4> { static constexpr int TX = 128, TY = 16, RY = 1, NS = 8; };
-template <int R>
-using B1Shape = StreamShape<R, B1S<R>::TX, B1S<R>::TY, B1S<R>::RY, B1S<R>::NS>;
+// Stream shapes of the batch kernel per radius: the persistent single-grid
+// defaults (one row per thread at R = 1, 3, 4; two rows per thread at R = 2)
+// with 15 consumer warps instead of 16 (tiles of 15 or 30 rows), so that the
+// block is 16 warps: four per SM sub-partition leave 128 registers a thread
+// (17 warps would leave 96, too few for the code of every radius in one
+// kernel without spills).
+// N: narrow tiles (64 x 30) for grids at most 64 cells wide at R <= 2, where
+// a 128-wide tile would leave most consumer threads without cells.
+template <int R, bool N = false> struct B1S;
+template <> struct B1S<1, false> { static constexpr int TX = 128, TY = 15, RY = 1, NS = 16; };
+template <> struct B1S<2, false> { static constexpr int TX = 128, TY = 30, RY = 2, NS = 8; };
+template <> struct B1S<3, false> { static constexpr int TX = 128, TY = 15, RY = 1, NS = 8; };
+template <> struct B1S<4, false> { static constexpr int TX = 128, TY = 15, RY = 1, NS = 8; };
+template <> struct B1S<1, true> { static constexpr int TX = 64, TY = 30, RY = 1, NS = 16; };
+template <> struct B1S<2, true> { static constexpr int TX = 64, TY = 30, RY = 1, NS = 16; };
+template <int R, bool N = false>
+using B1Shape = StreamShape<R, B1S<R, N>::TX, B1S<R, N>::TY, B1S<R, N>::RY, B1S<R, N>::NS>;
 
-constexpr int kB1Threads = 544;
+constexpr int kB1Threads = 512;
 static_assert(B1Shape<1>::THREADS == kB1Threads && B1Shape<2>::THREADS == kB1Threads &&
-                  B1Shape<3>::THREADS == kB1Threads && B1Shape<4>::THREADS == kB1Threads,
+                  B1Shape<3>::THREADS == kB1Threads && B1Shape<4>::THREADS == kB1Threads &&
+                  B1Shape<1, true>::THREADS == kB1Threads && B1Shape<2, true>::THREADS == kB1Threads,
               "every stream shape of the batch kernel has the kernel's block size");
 constexpr int kB1MaxSlots = 16;   // mbarriers: full[16], empty[16], swept
 constexpr int kB1BarBytes = 384;  // (2 * 16 + 1) * 8 rounded up to 128
-template <int R>
-constexpr int b1_ring_bytes() { return B1S<R>::NS * B1Shape<R>::SLOT_FLOATS * 4; }
+template <int R, bool N = false>
+constexpr int b1_ring_bytes() { return B1S<R, N>::NS * B1Shape<R, N>::SLOT_FLOATS * 4; }
 constexpr int kB1RingBytes =
-    std::max(std::max(b1_ring_bytes<1>(), b1_ring_bytes<2>()), std::max(b1_ring_bytes<3>(), b1_ring_bytes<4>()));
+    std::max(std::max(std::max(b1_ring_bytes<1>(), b1_ring_bytes<2>()), std::max(b1_ring_bytes<3>(), b1_ring_bytes<4>())),
+             std::max(b1_ring_bytes<1, true>(), b1_ring_bytes<2, true>()));
 constexpr int kB1Smem = 128 + kB1BarBytes + kB1RingBytes;
-static_assert(B1S<1>::NS <= kB1MaxSlots && B1S<2>::NS <= kB1MaxSlots, "ring fits the mbarrier area");
+static_assert(B1S<1>::NS <= kB1MaxSlots && B1S<2>::NS <= kB1MaxSlots && B1S<1, true>::NS <= kB1MaxSlots &&
+                  B1S<2, true>::NS <= kB1MaxSlots,
+              "ring fits the mbarrier area");
+
+// 2-D grids read with plain (L1-cached) loads: every read of another CTA's
+// writes follows the team barrier's acquire and a CTA barrier (GB300, the
+// 512-grid benchmark batch: its 2-D grids from 640^2 up 0.94 -> 0.82 s, those
+// below 0.154 -> 0.122 s, against ld.global.cg).  0 selects ld.global.cg.
+#ifndef STENCIL_B1_ROWS_L1
+#define STENCIL_B1_ROWS_L1 1
+#endif
 
 constexpr int kB1MaxTiers = 12;
 constexpr int kB1MaxCtas = 1024;
@@ -78,6 +97,7 @@ struct B1Job {
     Geom g;                // g.sy: row pitch of a and b (a multiple of 4)
     int dims, iters;
     int map_pair;          // 3-D: its tensor maps (a, b) are maps[2 * map_pair] and the next, else -1
+    int narrow;            // 3-D: swept with the narrow tiles of its radius
     int tiles_x, tiles_y, zchunk, items;  // 3-D work items for its tier's team size
     int hb, nblk;          // 2-D row blocks for its tier's team size
     long long rows;        // rows of the grid (ny * nz)
@@ -239,11 +259,11 @@ __device__ __forceinline__ void next_job(const B1Args &A, B1Ctl &c) {
 // would let the others' producers pass a sweep barrier early.  The ring's mbarriers are set up afresh for the
 // grid's shape (those of the previous grid, all of whose phases completed
 // before the CTA barrier that ended it, are invalidated first).
-template <int R>
+template <int R, bool N>
 __device__ __forceinline__ void job3d(const B1Args &A, const B1Job *__restrict__ J, unsigned char *base,
                                       B1Ctl &c) {
-    using Sh = B1S<R>;
-    using S = B1Shape<R>;
+    using Sh = B1S<R, N>;
+    using S = B1Shape<R, N>;
     const unsigned P = min((unsigned)J->items, c.size);
     __syncthreads();
     if (c.rel < P) {
@@ -287,7 +307,8 @@ __device__ __forceinline__ bool job2d(const B1Args &A, const B1Job *__restrict__
     for (int sw = 0; sw < iters; ++sw) {
         const float *src = (sw & 1) ? J->b : J->a;
         float *dst = (sw & 1) ? J->a : J->b;
-        rows2d_sweep<R, kB1Threads>(src, dst, J->g, J->hb, J->nblk, c.rel, c.size);
+        rows2d_sweep_d<R, kB1Threads, (R == 1 ? 4 : R == 2 ? 2 : 1), STENCIL_B1_ROWS_L1 != 0>(
+            src, dst, J->g, J->hb, J->nblk, c.rel, c.size);
         if (sw + 1 < iters && !team_barrier(A, c)) return false;
     }
     return true;
@@ -302,11 +323,13 @@ __device__ __forceinline__ bool run_job(const B1Args &A, const B1Job *__restrict
         if (!team_barrier(A, c)) return false;
     }
     if (J->dims == 3) {
-        switch (J->g.radius) {
-            case 1: job3d<1>(A, J, base, c); break;
-            case 2: job3d<2>(A, J, base, c); break;
-            case 3: job3d<3>(A, J, base, c); break;
-            default: job3d<4>(A, J, base, c); break;
+        switch (J->g.radius * 2 + (J->narrow ? 1 : 0)) {
+            case 2: job3d<1, false>(A, J, base, c); break;
+            case 3: job3d<1, true>(A, J, base, c); break;
+            case 4: job3d<2, false>(A, J, base, c); break;
+            case 5: job3d<2, true>(A, J, base, c); break;
+            case 6: job3d<3, false>(A, J, base, c); break;
+            default: job3d<4, false>(A, J, base, c); break;
         }
     } else {
         bool ok;
@@ -409,14 +432,16 @@ long long env_ll(const char *name, long long dflt) {
 
 }  // namespace
 
-// Update cells per CTA per sweep that a team keeps (defaults measured on
-// GB300 with the 512-grid benchmark batch; environment variables of the
-// same names override them at prepare time), and the largest team.
+// Update cells per CTA per sweep that a team keeps, and the largest team
+// (environment variables of the same names override them at prepare time).
+// GB300, the 512-grid benchmark batch, seconds per batch for 2-D / 3-D
+// cells per CTA: 25k/50k 2.79, 50k/50k 2.76, 50k/100k 2.90, 100k/100k 3.06,
+// 100k/200k 3.36 (before the L1-cached 2-D loads; with them 50k/50k 2.63).
 #ifndef STENCIL_BATCH1_CELLS_PER_CTA_2D
-#define STENCIL_BATCH1_CELLS_PER_CTA_2D 100000
+#define STENCIL_BATCH1_CELLS_PER_CTA_2D 50000
 #endif
 #ifndef STENCIL_BATCH1_CELLS_PER_CTA_3D
-#define STENCIL_BATCH1_CELLS_PER_CTA_3D 200000
+#define STENCIL_BATCH1_CELLS_PER_CTA_3D 50000
 #endif
 
 size_t batch1_bytes_for(const stencil_batch_job *jobs, int njobs) {
@@ -495,10 +520,13 @@ int batch1_prepare(const stencil_batch_job *jobs, int njobs, void *d_workspace,
         const int team = ladder[t];
         if (p.dims == 3) {
             int tx = 0, ty = 0;
-            switch (p.radius) {
-                case 1: tx = B1S<1>::TX; ty = B1S<1>::TY; break;
-                case 2: tx = B1S<2>::TX; ty = B1S<2>::TY; break;
-                case 3: tx = B1S<3>::TX; ty = B1S<3>::TY; break;
+            J.narrow = p.radius <= 2 && p.nx <= 64;
+            switch (p.radius * 2 + J.narrow) {
+                case 2: tx = B1S<1>::TX; ty = B1S<1>::TY; break;
+                case 3: tx = B1S<1, true>::TX; ty = B1S<1, true>::TY; break;
+                case 4: tx = B1S<2>::TX; ty = B1S<2>::TY; break;
+                case 5: tx = B1S<2, true>::TX; ty = B1S<2, true>::TY; break;
+                case 6: tx = B1S<3>::TX; ty = B1S<3>::TY; break;
                 default: tx = B1S<4>::TX; ty = B1S<4>::TY; break;
             }
             stream3d_plan(g, tx, ty, team, &J.tiles_x, &J.tiles_y, &J.zchunk, &J.items);

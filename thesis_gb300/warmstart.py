@@ -55,7 +55,7 @@ def run_batch(grids_a, grids_b, sweeps, cluster_size=0):
     """Runs `sweeps` Jacobi sweeps on each grid pair in one persistent launch;
     returns the tensors holding the results."""
     jobs = [(a, b, 1, int(sweeps), _lib.MODE_JACOBI) for a, b in zip(grids_a, grids_b)]
-    bt = S.Batch(jobs, cluster_size=cluster_size)
+    bt = S.Batch(jobs, cluster_size=cluster_size, engine="phased")
     bt.launch()
     res = [bt.result(k) for k in range(len(jobs))]
     bt.close()
