@@ -464,7 +464,9 @@ def c4_jobs(seed=20251204):
 def bench_c4(S, lib, torch):
     """512 grids of uneven sizes and sweep counts.  The line item: the
     one-launch engine -- every grid in ONE cooperative launch, teams of CTAs
-    taking grids from device queues -- replayed as a CUDA graph.  Beside it
+    taking grids from device queues -- with the team sizes the autotuner
+    picks per class of grid, replayed as a CUDA graph (its default team
+    sizes are reported too).  Beside it
     the phased engine (a persistent cluster launch over a device work queue
     for the grids a cluster sweeps, then persistent whole-GPU launches in
     lanes), with its cluster size and per-class hints picked by the
@@ -503,7 +505,21 @@ def bench_c4(S, lib, torch):
         return min(times)
 
     jobs = [(g[0], g[1], sp[1], sp[2], lib.MODE_JACOBI) for g, sp in zip(grids, specs)]
+
+    def class_jobs(cls):
+        # up to 6 grids of the class with a tenth of their sweeps: the proxy
+        # the tuners time (fresh copies, so the benchmark grids stay as made)
+        ks = [k for k, sp in enumerate(specs) if A.batch_class(sp[0]) == cls][:6]
+        return [(grids[k][0].clone(), grids[k][1].clone(), specs[k][1],
+                 max(10, specs[k][2] // 10), lib.MODE_JACOBI) for k in ks]
+
+    # the one-launch engine with its default team sizes, and with the team
+    # sizes the autotuner picks per class on the proxies (the line item)
     b1 = S.Batch(jobs, engine="one_launch")
+    t1_default = timed(b1)
+    b1.close()
+    teams_tuned = A.tune_batch_teams(class_jobs, log=None)
+    b1 = S.Batch(jobs, engine="one_launch", hints_for=A.batch_team_hints({"batch_one_launch": teams_tuned}))
     t1 = timed(b1)
     launches1, teams = b1.kernel_launches(), b1.teams()
     b1.close()
@@ -514,14 +530,6 @@ def bench_c4(S, lib, torch):
                 for k in range(0, len(specs), 8)]
 
     csize, _ = A.tune_batch_cluster_size(sample_jobs, log=None)
-
-    def class_jobs(cls):
-        # up to 6 grids of the class with a tenth of their sweeps: the proxy
-        # the tuner times (fresh copies, so the benchmark grids stay as made)
-        ks = [k for k, sp in enumerate(specs) if A.batch_class(sp[0]) == cls][:6]
-        return [(grids[k][0].clone(), grids[k][1].clone(), specs[k][1],
-                 max(10, specs[k][2] // 10), lib.MODE_JACOBI) for k in ks]
-
     tuned = A.tune_batch(class_jobs, log=None)
     bt = S.Batch(jobs, cluster_size=csize, hints_for=A.batch_hints({"batch": tuned}), engine="phased")
     tp = timed(bt)
@@ -538,6 +546,8 @@ def bench_c4(S, lib, torch):
             "s_per_batch": round(t1, 3), "cell_updates": ups, "engine": "one_launch",
             "device_bytes": mem, "graph_replays_per_batch": 1, "kernel_launches_per_batch": launches1,
             "teams": [{"team_ctas": t, "jobs": n} for t, n in teams], "graph": True,
+            "tuned_cells_per_cta": {c: r["choice"]["cells_per_cta"] for c, r in teams_tuned.items()},
+            "default_teams": {"value": round(ups / t1_default / 1e9, 2), "s_per_batch": round(t1_default, 3)},
             "roofline_frac_if_hbm": round(ups / t1 * 8 / 1e9 / peaks()[0], 4),
             "phased": {"value": round(ups / tp / 1e9, 2), "s_per_batch": round(tp, 3),
                        "kernel_launches_per_batch": launches, "cluster_jobs": cluster_jobs,

@@ -176,9 +176,14 @@ typedef struct stencil_batch_job {
      * temporally blocked engine's depth, and for a 3-D one with a whole-GPU
      * launch >= 2 selects the temporally blocked kernel with that depth (R
      * <= 2, JACOBI; else the one-sweep-per-pass stream kernel);
-     * tile_x, tile_y: the 2-D whole-GPU engine's tile in cells. */
+     * tile_x, tile_y: the 2-D whole-GPU engine's tile in cells.
+     * These three are used by the phased engine.  team: the CTAs the
+     * one-launch engine gives this grid (rounded down to one of its team
+     * sizes, the device's CTA count halved repeatedly; 0 = from the grid's
+     * cells), ignored by the phased engine. */
     int temporal, tile_x, tile_y;
-    int reserved[3]; /* must be zero */
+    int team;
+    int reserved[2]; /* must be zero */
 } stencil_batch_job;
 
 /* Device workspace bytes for njobs jobs whose nx are multiples of 4 (a job
@@ -232,7 +237,7 @@ STENCIL_API int stencil_batch_launch(const void *d_workspace, stencil_stream_t s
  * variables of these names override them at prepare time), every team
  * starts in the largest tier and splits into the next tier's teams when its
  * queue is empty; ragged grids are copied in and out by their team inside the
- * launch.  The tuning hints of stencil_batch_job are not used by it.  AUTO:
+ * launch.  It uses the jobs' team fields, not temporal / tile_x / tile_y.  AUTO:
  * the environment variable STENCIL_BATCH_ENGINE ("phased" or "one_launch")
  * at prepare time, else PHASED when some job carries tuning hints, else
  * ONE_LAUNCH. */

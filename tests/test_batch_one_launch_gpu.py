@@ -187,3 +187,42 @@ def test_one_launch_batch_reprepare_and_env_engine(cuda, monkeypatch):
     lib = L.load()
     rc = lib.stencil_batch_prepare_engine(None, 0, 3, 0, b.workspace.data_ptr(), 0, None)
     assert rc == L.EINVAL
+
+
+def test_one_launch_team_tuner_and_tuned_batch_match_oracle(cuda):
+    """The team-size tuner on per-class proxies, then the batch with its
+    team fields (AUTO still picks the one-launch engine for team-only hints):
+    bit-exact against the oracle; a team field beyond the device's CTAs is
+    clamped."""
+    import torch
+    from thesis_gb300 import autotune as A
+    from thesis_gb300 import stencil as S
+    specs = [((96, 100), 1, 9, "jacobi"), ((301, 257), 1, 7, "jacobi"), ((700, 720), 1, 5, "jacobi"),
+             ((1030, 1024), 1, 4, "jacobi"), ((40, 36, 44), 2, 6, "jacobi"), ((64, 64, 64), 2, 5, "jacobi"),
+             ((120, 112, 108), 2, 4, "jacobi"), ((130, 128, 126), 2, 3, "jacobi")]
+    hosts, jobs, modes = _make(specs, 1300)
+
+    def make(cls):
+        return [(j[0].clone(), j[1].clone()) + tuple(j[2:]) for j, sp in zip(jobs, specs)
+                if A.batch_class(sp[0]) == cls]
+
+    tuned = A.tune_batch_teams(make, repeats=1, log=None)
+    assert set(tuned) == {"2d_small", "2d_large", "3d_small", "3d_large"}
+    for r in tuned.values():
+        assert r["choice"]["cells_per_cta"] in A.BATCH1_SPACE["2d_small"]["cells_per_cta"]
+        assert r["s"] < float("inf") and r["default_s"] < float("inf")
+    b = S.Batch(jobs, hints_for=A.batch_team_hints({"batch_one_launch": tuned}))
+    assert b.kernel_launches() == 1 and b.teams()
+    b.launch()
+    torch.cuda.synchronize()
+    _check(b, specs, _wants(specs, hosts, modes), jobs)
+    b.close()
+    # a team field larger than the device's CTA count is clamped to it
+    _reset(jobs, hosts)
+    b = S.Batch([j + ({"team": 100000},) for j in jobs], engine="one_launch")
+    assert max(t for t, _ in b.teams()) <= torch.cuda.get_device_properties(0).multi_processor_count * 8
+    b.launch()
+    torch.cuda.synchronize()
+    _check(b, specs, _wants(specs, hosts, modes), jobs)
+    b.close()
+    assert S.device_status() == 0

@@ -326,6 +326,105 @@ def tune_batch(make_jobs, classes=None, repeats=2, log=print):
     return out
 
 
+# ---- batches, one-launch engine: CTAs per grid ----------------------------
+#
+# The one-launch engine gives each grid a team of CTAs (the device's CTA
+# count halved repeatedly); its default is the grid's update cells / 50000.
+# The tuner picks, per class of grid, the cells per CTA that set each grid's
+# team field (cells of the whole grid, border included).
+BATCH1_SPACE = {cls: {"cells_per_cta": [12500, 25000, 50000, 100000, 200000]}
+                for cls in ("2d_small", "2d_large", "3d_small", "3d_large")}
+
+
+def team_for(shape, cells_per_cta) -> int:
+    """The team field for a grid: its cells / cells_per_cta, at least one CTA
+    (the library rounds it down to a team size it has)."""
+    n = 1
+    for d in shape:
+        n *= d
+    return max(1, n // int(cells_per_cta))
+
+
+def batch_team_hints(db):
+    """hints_for(shape) -> {"team": ...} for thesis_gb300.stencil.Batch from a
+    database's "batch_one_launch" section (None for classes it does not
+    cover)."""
+    table = (db or {}).get("batch_one_launch", {})
+
+    def hints_for(shape):
+        c = table.get(batch_class(shape), {}).get("choice")
+        return {"team": team_for(shape, c["cells_per_cta"])} if c else None
+    return hints_for
+
+
+def tune_batch_teams(make_jobs, classes=None, repeats=2, time_batch=None, log=print):
+    """Per-class tuning of the one-launch engine's team sizes: make_jobs(cls)
+    returns fresh (d_u1, d_u2, radius, iterations, mode) jobs of that class (a
+    proxy of the batch).  Each candidate of BATCH1_SPACE sets every grid's
+    team field; its score is the CUDA-event time of one launch (min over
+    repeats), and a candidate whose results differ in any bit from the first
+    one's is rejected.  time_batch(jobs_with_hints) -> (seconds, results)
+    replaces the GPU timing (for tests).  Returns {class: {"choice":
+    {"cells_per_cta": n}, "s": seconds, "default_s": ...}}."""
+    def gpu_time(jobs):
+        import torch
+        from . import stencil as S
+        bt = S.Batch(jobs, engine="one_launch")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        bt.launch()
+        e1.record()
+        e1.synchronize()
+        res = [bt.result(k).clone() for k in range(len(jobs))]
+        bt.close()
+        return e0.elapsed_time(e1) / 1e3, res
+
+    time_batch = time_batch or gpu_time
+    out = {}
+    for cls in classes or list(BATCH1_SPACE):
+        jobs = make_jobs(cls)
+        if not jobs:
+            continue
+        init = [(j[0].clone(), j[1].clone()) for j in jobs]
+        ref = None
+
+        def score(cfg):
+            nonlocal ref
+            best, res = float("inf"), None
+            for _ in range(repeats):
+                for (u1, u2), job in zip(init, jobs):
+                    job[0].copy_(u1)
+                    job[1].copy_(u2)
+                hinted = [tuple(j[:5]) + ({"team": team_for(tuple(j[0].shape), cfg["cells_per_cta"])},)
+                          for j in jobs]
+                try:
+                    t, res = time_batch(hinted)
+                except _lib.StencilError:
+                    return float("inf")
+                best = min(best, t)
+            if ref is None:
+                ref = res
+            elif any(not _bits_equal(x, y) for x, y in zip(res, ref)):
+                return float("inf")
+            return best
+
+        start = {"cells_per_cta": 50000}
+        default_s = score(start)  # also records the reference results
+        best, best_s, n = coordinate_descent(start, dict(BATCH1_SPACE[cls]), score)
+        out[cls] = {"choice": {"cells_per_cta": best["cells_per_cta"]}, "s": best_s,
+                    "default_s": default_s, "candidates": n, "jobs": len(jobs)}
+        if log:
+            log("batch (one launch) %s: %s %.4f s (default %.4f s, %d candidates)"
+                % (cls, out[cls]["choice"], best_s, default_s, n))
+        del jobs, init, ref
+    return out
+
+
+def _bits_equal(x, y):
+    import torch
+    return x.shape == y.shape and torch.equal(x.contiguous().view(torch.int32), y.contiguous().view(torch.int32))
+
+
 def main():
     ap = argparse.ArgumentParser(description="tune the sweep kernels for one workload")
     ap.add_argument("--shape", type=int, nargs="+", required=True)

@@ -512,7 +512,10 @@ int batch1_prepare(const stencil_batch_job *jobs, int njobs, void *d_workspace,
         J.g = g;
         const long long cells = (long long)(p.nx - 2 * p.radius) * (p.ny - 2 * p.radius) *
                                 (p.dims == 3 ? p.nz - 2 * p.radius : 1);
-        const long long want = std::max(1LL, std::min(kmax, cells / (p.dims == 3 ? cpc3 : cpc2)));
+        // the job's own team size (a tuner's choice), else from its cells
+        const long long want =
+            b.team > 0 ? std::min<long long>(b.team, grid)
+                       : std::max(1LL, std::min(kmax, cells / (p.dims == 3 ? cpc3 : cpc2)));
         int t = 0;
         while (ladder[t] > want) ++t;
         tier_of[i] = t;

@@ -1005,10 +1005,10 @@ int check_batch_job(const stencil_batch_job &b, int i, stencil_params *out) {
     const int px = (b.nx + 3) & ~3;
     if (!cluster_job_ok(b.dims, px, b.ny, b.nz, b.radius))
         return fail(STENCIL_EUNSUPPORTED, "job %d: batch jobs need radius <= 4", i);
-    if (b.temporal < 0 || b.tile_x < 0 || b.tile_y < 0 || (b.tile_x % 4) || b.reserved[0] ||
-        b.reserved[1] || b.reserved[2])
+    if (b.temporal < 0 || b.tile_x < 0 || b.tile_y < 0 || (b.tile_x % 4) || b.team < 0 ||
+        b.reserved[0] || b.reserved[1])
         return fail(STENCIL_EINVAL,
-                    "job %d: temporal, tile_x, tile_y >= 0, tile_x %% 4 == 0, reserved zero", i);
+                    "job %d: temporal, tile_x, tile_y, team >= 0, tile_x %% 4 == 0, reserved zero", i);
     *out = p;
     return STENCIL_OK;
 }

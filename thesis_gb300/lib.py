@@ -40,7 +40,7 @@ class BatchJob(ctypes.Structure):
         ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
         ("radius", ctypes.c_int), ("iterations", ctypes.c_int), ("mode", ctypes.c_int),
         ("temporal", ctypes.c_int), ("tile_x", ctypes.c_int), ("tile_y", ctypes.c_int),
-        ("reserved", ctypes.c_int * 3),
+        ("team", ctypes.c_int), ("reserved", ctypes.c_int * 2),
     ]
 
 

@@ -240,7 +240,8 @@ class Batch:
 
     jobs: list of (d_u1, d_u2, radius, iterations, mode[, hints]) with CUDA
     float32 tensors of shape (ny, nx) or (nz, ny, nx); hints (optional dict)
-    sets the job's tuning fields "temporal" and "tile" (tile_x, tile_y).
+    sets the job's tuning fields "temporal" and "tile" (tile_x, tile_y; the
+    phased engine's) and "team" (the one-launch engine's CTAs for the grid).
     hints_for(shape) -> dict, when given, supplies hints for jobs without
     their own (e.g. autotune.batch_hints of a tuning database).  After
     ``launch`` each job's result is in d_u1 for an even sweep count, else in
@@ -259,6 +260,7 @@ class Batch:
             if h:
                 arr[k].temporal = int(h.get("temporal", 0))
                 arr[k].tile_x, arr[k].tile_y = (int(v) for v in h.get("tile", (0, 0)))
+                arr[k].team = int(h.get("team", 0))
             _check_tensor(u1)
             _check_tensor(u2, u1.shape)
             j = arr[k]
