@@ -514,11 +514,18 @@ def bench_c4(S, lib, torch):
                  max(10, specs[k][2] // 10), lib.MODE_JACOBI) for k in ks]
 
     # the one-launch engine with its default team sizes, and with the team
-    # sizes the autotuner picks per class on the proxies (the line item)
+    # sizes the autotuner picks per class on a proxy of the batch (the line
+    # item)
     b1 = S.Batch(jobs, engine="one_launch")
     t1_default = timed(b1)
     b1.close()
-    teams_tuned = A.tune_batch_teams(class_jobs, log=None)
+    def proxy_jobs():
+        # every grid with a tenth of its sweeps: the proxy the team tuner
+        # times (the classes share the GPU in one launch)
+        return [(g[0].clone(), g[1].clone(), sp[1], max(10, sp[2] // 10), lib.MODE_JACOBI)
+                for g, sp in zip(grids, specs)]
+
+    teams_tuned = A.tune_batch_teams(proxy_jobs, log=None)
     b1 = S.Batch(jobs, engine="one_launch", hints_for=A.batch_team_hints({"batch_one_launch": teams_tuned}))
     t1 = timed(b1)
     launches1, teams = b1.kernel_launches(), b1.teams()

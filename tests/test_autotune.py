@@ -95,30 +95,31 @@ def test_search_space_covers_3d_temporal_blocking_and_batch_classes():
 
 def test_team_tuner_picks_fastest_and_rejects_changed_results():
     """The one-launch engine's team tuner over BATCH1_SPACE with a stand-in
-    timer: the fastest candidate wins unless its results differ in a bit
-    from the first candidate's, and the database section maps every grid of
-    the class to its team field."""
+    timer: coordinate descent over the classes present in the proxy batch
+    finds the fastest combination, a candidate whose results differ in a bit
+    from the default's is rejected, and the database section maps every grid
+    of a class to its team field."""
     import torch
-    jobs = [(torch.zeros(1000, 1000), torch.zeros(1000, 1000), 1, 10, 1),
-            (torch.zeros(800, 900), torch.zeros(800, 900), 1, 7, 1)]
+    jobs = [(torch.zeros(1000, 1000), torch.zeros(1000, 1000), 1, 10, 1),   # 2d_large
+            (torch.zeros(100, 100), torch.zeros(100, 100), 1, 7, 1)]        # 2d_small
     seen = []
 
     def fake(hinted):
-        teams = [h[5]["team"] for h in hinted]
-        seen.append(teams[0])
-        # cells 1e6: 12500 -> 80, 25000 -> 40, 50000 -> 20, 100000 -> 10, 200000 -> 5
-        t = {80: 5.0, 40: 1.0, 20: 4.0, 10: 2.0, 5: 3.0}[teams[0]]
-        res = [torch.ones(3)]
-        if teams[0] == 40:
-            res = [torch.full((3,), 2.0)]  # a candidate that changes the result
+        big, small = (h[5]["team"] for h in hinted)
+        seen.append((big, small))
+        # 1e6 cells: 12500 -> 80, 25000 -> 40, 50000 -> 20, 100000 -> 10, 200000 -> 5
+        t = {80: 5.0, 40: 1.0, 20: 4.0, 10: 2.0, 5: 3.0}[big] + (0.0 if small == 1 else 0.5)
+        res = [torch.ones(3), torch.ones(2)]
+        if big == 40:
+            res = [torch.full((3,), 2.0), torch.ones(2)]  # a candidate that changes a result
         return t, res
 
-    out = A.tune_batch_teams(lambda cls: [tuple(j) for j in jobs] if cls == "2d_large" else [],
-                             repeats=1, time_batch=fake, log=None)
-    assert set(out) == {"2d_large"}
+    out = A.tune_batch_teams(lambda: [tuple(j) for j in jobs], time_batch=fake, log=None)
+    assert set(out) == {"2d_large", "2d_small"}
     assert out["2d_large"]["choice"] == {"cells_per_cta": 100000}   # 40 is faster but wrong
+    assert out["2d_small"]["choice"]["cells_per_cta"] >= 12500       # 10^4 cells: team 1 for all
     assert out["2d_large"]["default_s"] == 4.0 and out["2d_large"]["s"] == 2.0
-    assert set(seen) == {80, 40, 20, 10, 5}
+    assert {b for b, _ in seen} == {80, 40, 20, 10, 5}
     hints = A.batch_team_hints({"batch_one_launch": out})
-    assert hints((2000, 2000)) == {"team": 40} and hints((64, 64)) is None
+    assert hints((2000, 2000)) == {"team": 40} and hints((64, 64, 64)) is None
     assert A.team_for((10, 10, 10), 50000) == 1 and A.team_for((200, 200, 200), 50000) == 160

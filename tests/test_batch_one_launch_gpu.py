@@ -190,7 +190,7 @@ def test_one_launch_batch_reprepare_and_env_engine(cuda, monkeypatch):
 
 
 def test_one_launch_team_tuner_and_tuned_batch_match_oracle(cuda):
-    """The team-size tuner on per-class proxies, then the batch with its
+    """The team-size tuner on a copy of the batch, then the batch with its
     team fields (AUTO still picks the one-launch engine for team-only hints):
     bit-exact against the oracle; a team field beyond the device's CTAs is
     clamped."""
@@ -202,11 +202,10 @@ def test_one_launch_team_tuner_and_tuned_batch_match_oracle(cuda):
              ((120, 112, 108), 2, 4, "jacobi"), ((130, 128, 126), 2, 3, "jacobi")]
     hosts, jobs, modes = _make(specs, 1300)
 
-    def make(cls):
-        return [(j[0].clone(), j[1].clone()) + tuple(j[2:]) for j, sp in zip(jobs, specs)
-                if A.batch_class(sp[0]) == cls]
+    def make():
+        return [(j[0].clone(), j[1].clone()) + tuple(j[2:]) for j in jobs]
 
-    tuned = A.tune_batch_teams(make, repeats=1, log=None)
+    tuned = A.tune_batch_teams(make, log=None)
     assert set(tuned) == {"2d_small", "2d_large", "3d_small", "3d_large"}
     for r in tuned.values():
         assert r["choice"]["cells_per_cta"] in A.BATCH1_SPACE["2d_small"]["cells_per_cta"]

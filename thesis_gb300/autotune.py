@@ -357,14 +357,17 @@ def batch_team_hints(db):
     return hints_for
 
 
-def tune_batch_teams(make_jobs, classes=None, repeats=2, time_batch=None, log=print):
-    """Per-class tuning of the one-launch engine's team sizes: make_jobs(cls)
-    returns fresh (d_u1, d_u2, radius, iterations, mode) jobs of that class (a
-    proxy of the batch).  Each candidate of BATCH1_SPACE sets every grid's
-    team field; its score is the CUDA-event time of one launch (min over
-    repeats), and a candidate whose results differ in any bit from the first
-    one's is rejected.  time_batch(jobs_with_hints) -> (seconds, results)
-    replaces the GPU timing (for tests).  Returns {class: {"choice":
+def tune_batch_teams(make_jobs, classes=None, repeats=1, time_batch=None, log=print):
+    """Tuning of the one-launch engine's team sizes: make_jobs() returns fresh
+    (d_u1, d_u2, radius, iterations, mode) jobs of the whole batch (a proxy,
+    e.g. its grids with a tenth of their sweeps: the classes share the GPU
+    in one launch, so each is tuned beside the others).  The cells per CTA
+    of each class present (BATCH1_SPACE) are chosen by coordinate descent
+    from the library's default, each candidate setting every grid's team
+    field and scored by the CUDA-event time of one launch (min over
+    repeats); a candidate whose results differ in any bit from the
+    default's is rejected.  time_batch(jobs_with_hints) -> (seconds,
+    results) replaces the GPU timing (for tests).  Returns {class: {"choice":
     {"cells_per_cta": n}, "s": seconds, "default_s": ...}}."""
     def gpu_time(jobs):
         import torch
@@ -375,48 +378,48 @@ def tune_batch_teams(make_jobs, classes=None, repeats=2, time_batch=None, log=pr
         bt.launch()
         e1.record()
         e1.synchronize()
-        res = [bt.result(k).clone() for k in range(len(jobs))]
+        res = [bt.result(k) for k in range(len(jobs))]
         bt.close()
         return e0.elapsed_time(e1) / 1e3, res
 
     time_batch = time_batch or gpu_time
-    out = {}
-    for cls in classes or list(BATCH1_SPACE):
-        jobs = make_jobs(cls)
-        if not jobs:
-            continue
-        init = [(j[0].clone(), j[1].clone()) for j in jobs]
-        ref = None
+    jobs = make_jobs()
+    if not jobs:
+        return {}
+    cls_of = [batch_class(tuple(j[0].shape)) for j in jobs]
+    present = [c for c in BATCH1_SPACE if c in set(cls_of) and (classes is None or c in classes)]
+    init = [(j[0].clone(), j[1].clone()) for j in jobs]
+    ref = None
 
-        def score(cfg):
-            nonlocal ref
-            best, res = float("inf"), None
-            for _ in range(repeats):
-                for (u1, u2), job in zip(init, jobs):
-                    job[0].copy_(u1)
-                    job[1].copy_(u2)
-                hinted = [tuple(j[:5]) + ({"team": team_for(tuple(j[0].shape), cfg["cells_per_cta"])},)
-                          for j in jobs]
-                try:
-                    t, res = time_batch(hinted)
-                except _lib.StencilError:
-                    return float("inf")
-                best = min(best, t)
+    def score(cfg):
+        nonlocal ref
+        best = float("inf")
+        for _ in range(repeats):
+            for (u1, u2), job in zip(init, jobs):
+                job[0].copy_(u1)
+                job[1].copy_(u2)
+            hinted = [tuple(j[:5]) + ({"team": team_for(tuple(j[0].shape), cfg[c])} if c in cfg else {},)
+                      for j, c in zip(jobs, cls_of)]
+            try:
+                t, res = time_batch(hinted)
+            except _lib.StencilError:
+                return float("inf")
             if ref is None:
-                ref = res
+                ref = [x.clone() for x in res]
             elif any(not _bits_equal(x, y) for x, y in zip(res, ref)):
                 return float("inf")
-            return best
+            best = min(best, t)
+        return best
 
-        start = {"cells_per_cta": 50000}
-        default_s = score(start)  # also records the reference results
-        best, best_s, n = coordinate_descent(start, dict(BATCH1_SPACE[cls]), score)
-        out[cls] = {"choice": {"cells_per_cta": best["cells_per_cta"]}, "s": best_s,
-                    "default_s": default_s, "candidates": n, "jobs": len(jobs)}
-        if log:
-            log("batch (one launch) %s: %s %.4f s (default %.4f s, %d candidates)"
-                % (cls, out[cls]["choice"], best_s, default_s, n))
-        del jobs, init, ref
+    start = {c: 50000 for c in present}
+    default_s = score(start)  # also records the reference results
+    space = {c: list(BATCH1_SPACE[c]["cells_per_cta"]) for c in present}
+    best, best_s, n = coordinate_descent(start, space, score)
+    out = {c: {"choice": {"cells_per_cta": best[c]}, "s": best_s, "default_s": default_s,
+               "candidates": n, "jobs": len(jobs)} for c in present}
+    if log:
+        log("batch (one launch): %s %.4f s (default %.4f s, %d candidates)"
+            % ({c: best[c] for c in present}, best_s, default_s, n))
     return out
 
 
