@@ -317,7 +317,9 @@ __device__ __forceinline__ bool job2d(const B1Args &A, const B1Job *__restrict__
 // One grid on the team: copies in, sweeps, a team barrier, copies out.
 __device__ __forceinline__ bool run_job(const B1Args &A, const B1Job *__restrict__ J,
                                         unsigned char *base, B1Ctl &c) {
-    if (J->iters <= 0) return true;
+    // A grid with no sweep still ends with a team barrier: the leader's next
+    // mailbox write must follow every member's read of this grid's index.
+    if (J->iters <= 0) return team_barrier(A, c);
     if (J->ua) {
         stage_rows(*J, true, c.rel, c.size);
         if (!team_barrier(A, c)) return false;
