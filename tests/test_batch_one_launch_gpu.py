@@ -225,3 +225,38 @@ def test_one_launch_team_tuner_and_tuned_batch_match_oracle(cuda):
     _check(b, specs, _wants(specs, hosts, modes), jobs)
     b.close()
     assert S.device_status() == 0
+
+
+def test_one_launch_batch_zero_sweep_grids_keep_teams_together(cuda, monkeypatch):
+    """Grids with no sweep between swept ones, all on large teams: every team
+    stays on one grid at a time (a zero-sweep grid ends with a team barrier),
+    over several CUDA-graph replays."""
+    import torch
+    from thesis_gb300 import stencil as S
+    monkeypatch.setenv("STENCIL_BATCH1_CELLS_PER_CTA_2D", "1")
+    monkeypatch.setenv("STENCIL_BATCH1_CELLS_PER_CTA_3D", "1")
+    specs = []
+    for k in range(24):
+        if k % 2:
+            specs.append(((64 + 8 * k, 60 + 4 * k), 1, 0, "jacobi"))
+        elif k % 4 == 0:
+            specs.append(((40 + k, 36, 44), 2, 3 + k % 5, "jacobi"))
+        else:
+            specs.append(((300 + 10 * k, 257), 1, 2 + k % 7, "jacobi"))
+    hosts, jobs, modes = _make(specs, 1700)
+    b = S.Batch(jobs, engine="one_launch")
+    wants = _wants(specs, hosts, modes)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        b.launch(stream=s)
+        s.synchronize()
+        with torch.cuda.graph(g, stream=s):
+            b.launch(stream=s)
+    for _ in range(4):
+        _reset(jobs, hosts)
+        g.replay()
+        torch.cuda.synchronize()
+        _check(b, specs, wants, jobs)
+    b.close()
+    assert S.device_status() == 0

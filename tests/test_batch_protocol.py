@@ -62,6 +62,7 @@ def cta_program(cta, grid, tiers, jobs, sh, plant_idle_arrivals=False, skip_empt
                 sh.mail[key] = j
                 yield
             yield from barrier(key)
+            yield  # the mailbox is read some time after the wait ends
             j = sh.mail[key]
             if j < tiers[t]["njobs"]:
                 job = tiers[t]["first"] + j
