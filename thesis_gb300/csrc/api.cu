@@ -9,6 +9,8 @@
 #include <mutex>
 #include <vector>
 
+#include <cstdlib>
+#include <string>
 #include "host.hpp"
 
 namespace st {
@@ -406,6 +408,28 @@ int stencil_dispatch_ex(const stencil_params *p, float *d_u1, float *d_u2,
     return STENCIL_OK;
 }
 
+namespace st {
+namespace {
+// The device-side address of a pinned (page-locked, mapped) host buffer of at
+// least `bytes` bytes, 16-byte aligned, or null: such a buffer is copied by
+// a kernel running on every SM over the host link (GB300, 512 MiB each way:
+// see the bench's e2e), any other by cudaMemcpyAsync.
+// STENCIL_HOST_COPY=engine keeps every transfer on the copy engines.
+const void *mapped_host(const void *h, size_t bytes) {
+    const char *e = std::getenv("STENCIL_HOST_COPY");
+    if (e && std::string(e) == "engine") return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    if (((reinterpret_cast<uintptr_t>(a.devicePointer) | bytes) & 15) != 0) return nullptr;
+    return a.devicePointer;
+}
+}  // namespace
+}  // namespace st
+
 int stencil_run_host_timed(const stencil_params *p, const float *h_in, float *h_out,
                            float *ms_total, float *ms_sweeps) {
     int rc = stencil_params_check(p);
@@ -418,8 +442,15 @@ int stencil_run_host_timed(const stencil_params *p, const float *h_in, float *h_
     DeviceWorkspace *w = nullptr;
     rc = ws_grids(dev, bytes, &w);
     if (rc) return rc;
+    const void *d_in = mapped_host(h_in, bytes);
+    void *d_out = const_cast<void *>(mapped_host(h_out, bytes));
     ST_CUDA(cudaEventRecord(w->ev[0], w->stream));
-    ST_CUDA(cudaMemcpyAsync(w->u[0], h_in, bytes, cudaMemcpyHostToDevice, w->stream));
+    if (d_in) {
+        rc = launch_copy16(w->u[0], d_in, bytes, w->stream);
+        if (rc) return rc;
+    } else {
+        ST_CUDA(cudaMemcpyAsync(w->u[0], h_in, bytes, cudaMemcpyHostToDevice, w->stream));
+    }
     if (p->mode == STENCIL_MODE_JACOBI)
         ST_CUDA(cudaMemcpyAsync(w->u[1], w->u[0], bytes, cudaMemcpyDeviceToDevice, w->stream));
     else
@@ -433,7 +464,15 @@ int stencil_run_host_timed(const stencil_params *p, const float *h_in, float *h_
         return rc;
     }
     ST_CUDA(cudaEventRecord(w->ev[3], w->stream));
-    ST_CUDA(cudaMemcpyAsync(h_out, res, bytes, cudaMemcpyDeviceToHost, w->stream));
+    if (d_out) {
+        rc = launch_copy16(d_out, res, bytes, w->stream);
+        if (rc) {
+            cudaStreamSynchronize(w->stream);
+            return rc;
+        }
+    } else {
+        ST_CUDA(cudaMemcpyAsync(h_out, res, bytes, cudaMemcpyDeviceToHost, w->stream));
+    }
     ST_CUDA(cudaEventRecord(w->ev[1], w->stream));
     ST_CUDA(cudaStreamSynchronize(w->stream));
     if (ms_total) ST_CUDA(cudaEventElapsedTime(ms_total, w->ev[0], w->ev[1]));

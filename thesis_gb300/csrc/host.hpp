@@ -136,6 +136,9 @@ int ir2_launch(const Geom &g, const Ir2Plan &p, float *u, unsigned long long *xc
 
 // Plain whole-grid helpers.
 int launch_copy_border(const Geom &g, int dims, const float *src, float *dst, cudaStream_t s);
+// Copies bytes (a multiple of 16, both addresses 16-byte aligned) with a
+// streaming kernel over every SM (k_util.cu).
+int launch_copy16(void *dst, const void *src, size_t bytes, cudaStream_t s);
 int launch_init_reference(const Geom &g, int dims, float *u, cudaStream_t s);
 
 }  // namespace st

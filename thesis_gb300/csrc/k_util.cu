@@ -295,4 +295,34 @@ int launch_residual(const Geom &g, int dims, const float *u, double *scratch, cu
 }
 
 
+// Streaming copy of n16 16-byte words, for host<->device transfers through
+// the device-side address of pinned (mapped) host memory: every SM pulls
+// (or pushes) over the C2C link instead of one copy engine.  Four loads per
+// thread in flight; loads and stores marked streaming (no L1 allocation).
+constexpr int kCopyThreads = 512;
+__global__ void __launch_bounds__(kCopyThreads)
+    k_copy16(float4 *__restrict__ dst, const float4 *__restrict__ src, size_t n16) {
+    const size_t stride = (size_t)gridDim.x * kCopyThreads;
+    size_t i = (size_t)blockIdx.x * kCopyThreads + threadIdx.x;
+    for (; i + 3 * stride < n16; i += 4 * stride) {
+        float4 v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] = __ldcs(src + i + k * stride);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) __stcs(dst + i + k * stride, v[k]);
+    }
+    for (; i < n16; i += stride) __stcs(dst + i, __ldcs(src + i));
+}
+
+int launch_copy16(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) | bytes) & 15) != 0)
+        return fail(STENCIL_EINVAL, "copy kernel: 16-byte aligned addresses and size required");
+    if (!bytes) return STENCIL_OK;
+    const size_t n16 = bytes / 16;
+    const int blocks = (int)std::min<size_t>((size_t)num_sms() * 4, (n16 + kCopyThreads - 1) / kCopyThreads);
+    k_copy16<<<blocks, kCopyThreads, 0, s>>>(static_cast<float4 *>(dst), static_cast<const float4 *>(src), n16);
+    ST_CUDA(cudaGetLastError());
+    return STENCIL_OK;
+}
+
 }  // namespace st
