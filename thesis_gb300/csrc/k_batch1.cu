@@ -15,7 +15,8 @@
 //
 // Teams and tiers.  The host puts each grid in a tier by the team size its
 // cells keep busy (about STENCIL_BATCH1_CELLS_PER_CTA_{2D,3D} update cells
-// per CTA per sweep, so the per-sweep barrier stays a small share); tier t has
+// per CTA per sweep, so the per-sweep barrier stays a small share), or by the
+// job's own team field (an autotuner's choice); tier t has
 // a nominal team size and a queue of its grids, largest work first.  All
 // CTAs start in the first tier as teams of its size; a team whose tier queue
 // is empty splits into the next tier's teams (its own CTAs: never waiting on
