@@ -260,3 +260,32 @@ def test_one_launch_batch_zero_sweep_grids_keep_teams_together(cuda, monkeypatch
         _check(b, specs, wants, jobs)
     b.close()
     assert S.device_status() == 0
+
+
+def test_one_launch_matches_phased_on_the_benchmark_batch(cuda):
+    """The 512-grid benchmark batch at full size (384 2-D R=1 grids of
+    64..2048, 128 3-D R=2 grids of 32..256, 100..5000 sweeps; 382 ragged
+    widths): the one-launch engine's results equal the phased engine's bit
+    for bit in every grid (the phased engine is pinned to the oracle above
+    and in test_cluster_gpu.py), with its default and with tuned-looking
+    team sizes."""
+    import torch
+    from bench import c4_jobs
+    from thesis_gb300 import lib as L
+    from thesis_gb300 import stencil as S
+    specs = c4_jobs()
+    init = [S.init_uniform(sp[0], 31 + k) for k, sp in enumerate(specs)]
+    outs = {}
+    for name, engine, hints in [("phased", "phased", None), ("one", "one_launch", None),
+                                ("one_teams", "one_launch", lambda shape: {"team": 38 if len(shape) == 3 else 9})]:
+        jobs = [(u.clone(), u.clone(), sp[1], sp[2], L.MODE_JACOBI) for u, sp in zip(init, specs)]
+        b = S.Batch(jobs, engine=engine, hints_for=hints)
+        b.launch()
+        torch.cuda.synchronize()
+        outs[name] = [b.result(k) for k in range(len(jobs))]
+        b.close()
+    for name in ("one", "one_teams"):
+        bad = [k for k in range(len(specs))
+               if not torch.equal(outs[name][k].view(torch.int32), outs["phased"][k].view(torch.int32))]
+        assert not bad, (name, bad[:5], [specs[k] for k in bad[:5]])
+    assert S.device_status() == 0
