@@ -123,3 +123,13 @@ def test_team_tuner_picks_fastest_and_rejects_changed_results():
     hints = A.batch_team_hints({"batch_one_launch": out})
     assert hints((2000, 2000)) == {"team": 40} and hints((64, 64, 64)) is None
     assert A.team_for((10, 10, 10), 50000) == 1 and A.team_for((200, 200, 200), 50000) == 160
+
+
+def test_coordinate_descent_min_gain_keeps_the_start_within_noise():
+    space = {"a": [1, 2, 3]}
+    score = {1: 1.0, 2: 0.995, 3: 0.98}
+    best, s, _ = A.coordinate_descent({"a": 1}, space, lambda c: score[c["a"]], min_gain=0.01)
+    assert best == {"a": 3} and s == 0.98          # 2 % better: taken
+    score[3] = 0.995
+    best, s, _ = A.coordinate_descent({"a": 1}, space, lambda c: score[c["a"]], min_gain=0.01)
+    assert best == {"a": 1} and s == 1.0           # 0.5 %: noise, the start stays
