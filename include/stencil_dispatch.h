@@ -255,7 +255,7 @@ STENCIL_API int stencil_batch_prepare_engine(const stencil_batch_job *jobs, int 
  * launch of their own (both 0 for the one-launch engine). */
 STENCIL_API int stencil_batch_plan(const void *d_workspace, int *cluster_jobs, int *whole_gpu_jobs);
 /* Kernel launches of one stencil_batch_launch of a prepared workspace (1 for
- * the one-launch engine). */
+ * the one-launch engine, 0 when it has no job). */
 STENCIL_API int stencil_batch_launches(const void *d_workspace, int *kernel_launches);
 /* The one-launch engine's tiers: *tiers of them (0 for a phased workspace),
  * the nominal team size and the job count of each of the first max_tiers in

@@ -109,6 +109,7 @@ int batch1_prepare(const stencil_batch_job *jobs, int njobs, void *d_workspace,
                    size_t workspace_bytes, cudaStream_t s);
 bool batch1_known(const void *d_workspace);
 int batch1_launch(const void *d_workspace, cudaStream_t s);
+int batch1_launches(const void *d_workspace);  // kernels per launch: 1, or 0 without jobs
 int batch1_teams(const void *d_workspace, int *ntiers, int *team_sizes, int *tier_jobs, int max_tiers);
 void batch1_forget(const void *d_workspace);
 

@@ -634,6 +634,11 @@ int batch1_launch(const void *d_workspace, cudaStream_t s) {
     return STENCIL_OK;
 }
 
+int batch1_launches(const void *d_workspace) {
+    B1Plan plan;
+    return b1_recall(d_workspace, &plan) && plan.njobs ? 1 : 0;
+}
+
 int batch1_teams(const void *d_workspace, int *ntiers, int *team_sizes, int *tier_jobs, int max_tiers) {
     B1Plan plan;
     if (!b1_recall(d_workspace, &plan)) return fail(STENCIL_EINVAL, "not a one-launch batch workspace");

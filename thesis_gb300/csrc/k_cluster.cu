@@ -1257,7 +1257,7 @@ extern "C" int stencil_batch_side_by_side(const void *d_workspace, int *groups, 
 extern "C" int stencil_batch_launches(const void *d_workspace, int *kernel_launches) {
     if (!d_workspace || !kernel_launches) return fail(STENCIL_EINVAL, "null argument");
     if (batch1_known(d_workspace)) {
-        *kernel_launches = 1;
+        *kernel_launches = batch1_launches(d_workspace);
         return STENCIL_OK;
     }
     BatchPlan plan;
