@@ -187,6 +187,13 @@ def test_one_launch_batch_reprepare_and_env_engine(cuda, monkeypatch):
     lib = L.load()
     rc = lib.stencil_batch_prepare_engine(None, 0, 3, 0, b.workspace.data_ptr(), 0, None)
     assert rc == L.EINVAL
+    # an empty batch: nothing to launch
+    monkeypatch.delenv("STENCIL_BATCH_ENGINE")
+    e = S.Batch([], engine="one_launch")
+    assert e.kernel_launches() == 0 and e.teams() == []
+    e.launch()
+    torch.cuda.synchronize()
+    e.close()
 
 
 def test_one_launch_team_tuner_and_tuned_batch_match_oracle(cuda):
