@@ -12,13 +12,15 @@
 // with a grid stride; consecutive threads take consecutive chunk columns, so
 // a warp's loads and stores are contiguous 512-byte segments.
 //
-// Loads use ld.global.cg (L2, not L1): a buffer is rewritten every other
-// sweep inside the launch, so a line kept in an SM's L1 from two sweeps back
-// would be stale.  Every cell keeps the reference's summation order (axis i
+// Loads are plain (L1-cached): a buffer is rewritten every other sweep
+// inside the launch, and every read of another CTA's writes follows the grid
+// barrier's acquire at GPU scope and a CTA barrier, after which weak loads
+// observe those writes (PTX memory model).  Every cell keeps the reference's summation order (axis i
 // offsets -R..-1, +1..+R, then axis j, from +0) and division, so results are
 // bit-identical to single sweeps; cells outside the update region are never
 // written.
 #include <algorithm>
+#include <cstdlib>
 #include <mutex>
 #include <vector>
 
@@ -30,14 +32,14 @@ namespace {
 
 constexpr int kRowsThreads = 512;
 
-template <int R>
+template <int R, bool L1>
 __global__ void __launch_bounds__(kRowsThreads, R <= 2 ? 2 : 1)
     k_rows2d(float *a, float *b, Geom g, int hb, int nblk, int iters, unsigned *bar) {
     __shared__ int s_ok;
     for (int sw = 0; sw < iters; ++sw) {
         const float *src = (sw & 1) ? b : a;
         float *dst = (sw & 1) ? a : b;
-        rows2d_sweep<R, kRowsThreads>(src, dst, g, hb, nblk, blockIdx.x, gridDim.x);
+        rows2d_sweep<R, kRowsThreads, L1>(src, dst, g, hb, nblk, blockIdx.x, gridDim.x);
         if (sw + 1 < iters) {
             // every CTA's writes of this sweep before any CTA's next reads
             __syncthreads();
@@ -53,14 +55,30 @@ __global__ void __launch_bounds__(kRowsThreads, R <= 2 ? 2 : 1)
 
 using RowsFn = void (*)(float *, float *, Geom, int, int, int, unsigned *);
 
-RowsFn rows_fn(int r) {
-    switch (r) {
-        case 1: return k_rows2d<1>;
-        case 2: return k_rows2d<2>;
-        case 3: return k_rows2d<3>;
-        case 4: return k_rows2d<4>;
+// Loads: plain, L1-cached (the x-neighbour chunks are other threads' centre
+// chunks of the same row), legal because every read of another CTA's writes
+// follows the grid barrier's acquire and a CTA barrier; STENCIL_ROWS_L1=0
+// (read at each launch) selects ld.global.cg.  GB300, R = 1, bit-identical:
+// 1024^2 309.5 -> 327.0, 1500^2 438.7 -> 493.0, 2048^2 575.1 -> 640.4,
+// 4096^2 626.1 -> 634.4, 8192^2 592.8 -> 596.1 GCell/s; R = 4 2048^2
+// 426.0 -> 445.0.
+RowsFn rows_fn(int r, bool l1 = false) {
+    switch (r * 2 + (l1 ? 1 : 0)) {
+        case 2: return k_rows2d<1, false>;
+        case 3: return k_rows2d<1, true>;
+        case 4: return k_rows2d<2, false>;
+        case 5: return k_rows2d<2, true>;
+        case 6: return k_rows2d<3, false>;
+        case 7: return k_rows2d<3, true>;
+        case 8: return k_rows2d<4, false>;
+        case 9: return k_rows2d<4, true>;
         default: return nullptr;
     }
+}
+
+bool rows_l1() {
+    const char *e = std::getenv("STENCIL_ROWS_L1");
+    return !(e && e[0] == '0');
 }
 
 // Resident CTAs of the radius-r kernel (once per radius and device).
@@ -122,7 +140,7 @@ int run_rows2d(const Geom &g, float *a, float *b, int iters, cudaStream_t s, flo
     Geom gg = g;
     int hb_ = hb, nb_ = nblk, n = iters;
     void *args[] = {&a, &b, &gg, &hb_, &nb_, &n, &bar};
-    ST_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(rows_fn(g.radius)), dim3(grid),
+    ST_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(rows_fn(g.radius, rows_l1())), dim3(grid),
                                         dim3(kRowsThreads), args, 0, s));
     note_launches("rows2d-persistent", 1);
     return STENCIL_OK;

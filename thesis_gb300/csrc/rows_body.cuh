@@ -9,10 +9,11 @@
 // 4-cell update costs three 16-byte loads at any R <= 4.  Items (chunk
 // column, row block) are spread over the nctas CTAs that share the grid with
 // a grid stride; consecutive threads take consecutive chunk columns, so a
-// warp's loads and stores are contiguous 512-byte segments.  Loads use
-// ld.global.cg (L2, not L1): a buffer is rewritten every other sweep inside
-// one launch, so a line kept in an SM's L1 from two sweeps back would be
-// stale.  Every cell keeps the reference's summation order (axis i offsets
+// warp's loads and stores are contiguous 512-byte segments.  Loads are
+// ld.global.cg (L2) or, with L1, plain L1-cached loads: a buffer is rewritten
+// every other sweep inside one launch, and the plain form relies on every
+// read of another CTA's writes following an acquire at GPU scope and a CTA
+// barrier (then weak loads observe those writes).  Every cell keeps the reference's summation order (axis i offsets
 // -R..-1, +1..+R, then axis j, from +0) and division; cells outside the
 // update region are never written.
 #pragma once
@@ -28,9 +29,14 @@ __device__ __forceinline__ float4 rows_ld4(const float *p) {
 // One sweep src -> dst of a 2-D grid (g.sy: the row pitch, a multiple of 4;
 // the chunk columns cover it) by CTA `cta` of the nctas CTAs of NT threads
 // that share it; hb rows per block, nblk blocks.
-template <int R, int NT>
+template <int R, int NT, bool L1 = false>
 __device__ __forceinline__ void rows2d_sweep(const float *src, float *dst, const Geom g, int hb,
                                              int nblk, unsigned cta, unsigned nctas) {
+    // L1: plain (L1-cached) loads instead of ld.global.cg (see rows2d_sweep_d)
+    auto rows_ld4 = [](const float *p) {
+        if constexpr (L1) return *reinterpret_cast<const float4 *>(p);
+        else return __ldcg(reinterpret_cast<const float4 *>(p));
+    };
     constexpr int C = 4 * R;
     constexpr int RA = (R + 3) & ~3;  // x halo in whole chunks (R <= 4: one chunk)
     static_assert(RA == 4, "one neighbour chunk per side");
