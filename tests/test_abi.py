@@ -168,3 +168,31 @@ def test_batch_engine_choice_is_validated_without_device(stencil_lib):
     assert stencil_lib.stencil_batch_workspace_bytes_for(jobs, 2, ctypes.byref(need)) == L.OK
     # two pitched copies of each ragged grid at least
     assert need.value >= 2 * 4 * (68 * 70 + 44 * 37 * 43)
+
+
+def test_one_launch_batch_jobs_are_checked_without_device(stencil_lib):
+    """The one-launch engine checks every job before it touches a device: a
+    negative team field, a nonzero reserved field, bad buffers or an odd tile
+    are refused with STENCIL_EINVAL; unknown workspaces are refused by the
+    queries."""
+    def job(**kw):
+        j = L.BatchJob()
+        j.d_u1, j.d_u2 = 4096, 8192
+        j.dims, j.nx, j.ny, j.nz, j.radius, j.iterations, j.mode = 2, 64, 64, 1, 1, 3, 1
+        for k, v in kw.items():
+            if k == "reserved":
+                j.reserved[0] = v
+            else:
+                setattr(j, k, v)
+        return j
+    ws = ctypes.c_void_p(1 << 20)
+    for bad, word in [(dict(team=-1), b"team"), (dict(reserved=1), b"reserved"),
+                      (dict(d_u2=4096), b"buffers"), (dict(tile_x=6), b"tile_x"),
+                      (dict(radius=5), b"radius")]:
+        jobs = (L.BatchJob * 2)(job(), job(**bad))
+        rc = stencil_lib.stencil_batch_prepare_engine(jobs, 2, 2, 0, ws, 1 << 30, None)
+        assert rc in (L.EINVAL, L.EUNSUPPORTED), bad
+        assert word in stencil_lib.stencil_last_error() and b"job 1" in stencil_lib.stencil_last_error(), bad
+    n = ctypes.c_int()
+    assert stencil_lib.stencil_batch_launches(ws, ctypes.byref(n)) == L.EINVAL
+    assert stencil_lib.stencil_batch_teams(ws, ctypes.byref(n), None, None, 0) == L.OK and n.value == 0

@@ -461,6 +461,12 @@ size_t batch1_bytes_for(const stencil_batch_job *jobs, int njobs) {
 // Validated jobs -> job table, tensor maps and tiers in the workspace.
 int batch1_prepare(const stencil_batch_job *jobs, int njobs, void *d_workspace,
                    size_t workspace_bytes, cudaStream_t s) {
+    // every job checked before anything reaches the device
+    for (int i = 0; i < njobs; ++i) {
+        stencil_params p;
+        const int rc = check_batch_job(jobs[i], i, &p);
+        if (rc) return rc;
+    }
     if (workspace_bytes < batch1_bytes_for(jobs, njobs))
         return fail(STENCIL_EINVAL, "workspace too small: %zu < %zu bytes (stencil_batch_workspace_bytes_for)",
                     workspace_bytes, batch1_bytes_for(jobs, njobs));
