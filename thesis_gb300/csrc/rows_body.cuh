@@ -13,18 +13,14 @@
 // ld.global.cg (L2) or, with L1, plain L1-cached loads: a buffer is rewritten
 // every other sweep inside one launch, and the plain form relies on every
 // read of another CTA's writes following an acquire at GPU scope and a CTA
-// barrier (then weak loads observe those writes).  Every cell keeps the reference's summation order (axis i offsets
-// -R..-1, +1..+R, then axis j, from +0) and division; cells outside the
-// update region are never written.
+// barrier (then weak loads observe those writes).  Every cell keeps the
+// reference's summation order (axis i offsets -R..-1, +1..+R, then axis j,
+// from +0) and division; cells outside the update region are never written.
 #pragma once
 
 #include "common.cuh"
 
 namespace st {
-
-__device__ __forceinline__ float4 rows_ld4(const float *p) {
-    return __ldcg(reinterpret_cast<const float4 *>(p));
-}
 
 // One sweep src -> dst of a 2-D grid (g.sy: the row pitch, a multiple of 4;
 // the chunk columns cover it) by CTA `cta` of the nctas CTAs of NT threads
