@@ -225,3 +225,104 @@ def test_protocol_catches_a_zero_sweep_grid_without_a_barrier():
         except AssertionError:
             caught += 1
     assert caught > 0
+
+
+def cta_program_bounded(cta, grid, tiers, jobs, sh, victim, die_after, limit):
+    """The protocol with the kernel's failure handling: every wait gives up
+    after `limit` steps (the kernel's bounded waits), sets the abort word and
+    ends the CTA; a leader that sees the abort word hands its team the stop
+    value instead of a grid.  CTA `victim` stops for good after `die_after`
+    of its own steps, arriving nowhere again (a CTA whose wait gave up)."""
+    steps = 0
+    t, start, size, rel, cnt, job = -1, 0, grid, 0, 0, STOP
+
+    def tick():
+        nonlocal steps
+        steps += 1
+        return cta == victim and steps > die_after
+
+    def barrier(key):
+        nonlocal cnt
+        sh.tbar[key] = sh.tbar.get(key, 0) + 1
+        cnt += size
+        spins = 0
+        while sh.tbar[key] < cnt:
+            spins += 1
+            if spins > limit:
+                sh.abort = True
+                return False
+            yield
+        return True
+
+    while True:
+        while True:
+            if t < 0 or job == STOP:
+                t += 1
+                if t >= len(tiers):
+                    return
+                start, size = split(start, size, tiers[t]["team"], cta)
+                rel, cnt = cta - start, 0
+            key = (t, start)
+            if tick():
+                return
+            if rel == 0:
+                if sh.abort:
+                    sh.mail[key] = "stop"
+                else:
+                    sh.mail[key] = sh.queue[t]
+                    sh.queue[t] += 1
+                yield
+            if not (yield from barrier(key)):
+                return
+            yield
+            j = sh.mail[key]
+            if j == "stop":
+                return
+            if j < tiers[t]["njobs"]:
+                job = tiers[t]["first"] + j
+                break
+            job = STOP
+        J = jobs[job]
+        sh.log.append(("begin", job, cta, int(sh.abort)))
+        for sw in range(max(1, J["iters"])):
+            if tick():
+                return
+            yield
+            if not (yield from barrier(key)):
+                return
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_protocol_a_stopped_cta_ends_the_launch_without_a_hang(seed):
+    """A CTA that stops mid-batch (its wait gave up): every other CTA ends
+    within bounded waits -- its teammates time out and set the abort word,
+    the other teams' leaders then hand out the stop value -- and no grid is
+    begun by part of a team (CPU emulation; the kernel's waits are bounded
+    by time)."""
+    rng = random.Random(100 + seed)
+    grid = rng.choice([8, 12, 16])
+    jobs = make_jobs(rng, 12)
+    tiers, jobs = plan(jobs, grid, lambda j: j["cells"] // 100000)
+    sh = Shared(len(tiers), grid)
+    sh.abort = False
+    victim = rng.randrange(grid)
+    progs = {c: cta_program_bounded(c, grid, tiers, jobs, sh, victim, rng.randint(1, 12), 400)
+             for c in range(grid)}
+    live = list(progs)
+    steps = 0
+    while live:
+        c = rng.choice(live)
+        try:
+            next(progs[c])
+        except StopIteration:
+            live.remove(c)
+        steps += 1
+        assert steps < 2_000_000, "a CTA never ended"
+    # every grid that began was handed out before its team's leader saw the
+    # abort word, so each was begun by its whole team or by none of it
+    begun = {}
+    for ev, j, c, _ in sh.log:
+        if ev == "begin":
+            begun.setdefault(j, set()).add(c)
+    for j, ctas in begun.items():
+        assert sorted(ctas) == list(range(min(ctas), max(ctas) + 1)), ("part of a team", j)
